@@ -1,0 +1,206 @@
+/*
+ * scs.h -- C ABI of the GB300 size-bounded community search engine.
+ *
+ * The reference (wajidmanzoor/SCS) has no library interface: its boundary is
+ * the server process.  Each entry point below replaces one piece of it:
+ *
+ *   scs_create / scs_create_csr  <- main.cu:475-585: graph load
+ *        (src/Graph.h:5-67), core decomposition (src/Graph.h:82-109), device
+ *        allocation (src/gpuMemoryAllocation.cc:22-165) from the 12 CLI args
+ *        (main.cu:476-502), here carried by scs_config.
+ *   scs_submit                   <- main.cu:62-78 + main.cu:84-119: one
+ *        "<l> <h> <qid> <heuristic_flag> <limit_dominating_set>" message
+ *        admitted into a query slot.
+ *   scs_run / scs_poll           <- main.cu:261-463: the level loop that runs
+ *        the search and writes one result row per finished query
+ *        (main.cu:122-133, 317-339, 340-360, 444-463).
+ *   scs_destroy                  <- main.cu:586-594 (free + device reset).
+ *
+ * Conventions: every call returns 0 or a negative SCS_E* code; nothing calls
+ * exit().  Plain pointers and sizes only.  One engine drives one GPU; calls on
+ * one engine must come from one thread at a time.
+ */
+#ifndef SCS_H
+#define SCS_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define SCS_OK 0
+#define SCS_EINVAL -1     /* bad argument */
+#define SCS_EIO -2        /* graph file missing or malformed */
+#define SCS_ECUDA -3      /* CUDA runtime error (message via scs_last_error) */
+#define SCS_ENOMEM -4     /* device or host allocation failed */
+#define SCS_EBUSY -5      /* no free query slot */
+#define SCS_ENOTREADY -6  /* nothing finished yet */
+
+/* ---- per-query result status (scs_result.status) ---- */
+#define SCS_DONE 0          /* search finished: degree is the optimum */
+#define SCS_HEURISTIC 1     /* answered by the greedy incumbent (kl == ku),
+                               the reference's Heu=1 row (main.cu:122-133) */
+#define SCS_CAPACITY 2      /* task store overflow: degree is the best found,
+                               the reference's Overtime=2 (main.cu:340-360) */
+#define SCS_TIMEOUT 3       /* stopped by the search budget: best found,
+                               the reference's Overtime=1 (main.cu:444-463) */
+#define SCS_BAD_QUERY 4     /* malformed query (main.cu:106-109) */
+#define SCS_TOO_LARGE 5     /* filtered graph exceeds the engine's limits */
+
+/* Engine configuration.  Field meanings follow the reference CLI where one
+ * exists (main.cu:476-502); zero selects the default. */
+typedef struct {
+  uint32_t limit_queries; /* concurrent query slots (CLI limitQueries)  */
+  uint32_t red1, red2, red3;  /* reduction rules on (1) / off (0)       */
+  uint32_t prun1, prun2;      /* upper-bound rules on (1) / off (0)     */
+  uint32_t rules_set;         /* 0: all rules on; 1: use the fields above */
+  uint32_t ctas_per_sm;       /* search CTAs per SM (0: auto)            */
+  uint32_t threads_per_cta;   /* 256 or 512 (0: auto)                    */
+  uint64_t stack_words;       /* task-stack words per CTA (0: auto)      */
+  uint64_t pool_words;        /* shared task-pool words (0: auto)        */
+  uint32_t slice_us;          /* search time slice in microseconds       */
+  uint64_t node_budget;       /* per-query task budget, 0 = unlimited
+                                 (stands in for the level cap main.cu:444) */
+  uint32_t host_threads;      /* threads for the greedy incumbent (0: auto) */
+  int32_t device;             /* CUDA device ordinal                      */
+} scs_config;
+
+/* One query: the reference's message fields (main.cu:92-119). */
+typedef struct {
+  uint32_t l;          /* lower size bound N1 */
+  uint32_t h;          /* upper size bound N2 */
+  uint32_t q;          /* query vertex QID */
+  uint32_t heuristic;  /* 1: greedy incumbent on (isHeu) */
+  uint32_t limit_doms; /* dominating-branch limit (limitDoms) */
+} scs_query;
+
+typedef struct {
+  uint64_t ticket;      /* value returned by scs_submit */
+  uint32_t l, h, q;     /* echo of the query */
+  uint32_t degree;      /* maximum minimum degree (Degree column) */
+  int32_t status;       /* SCS_DONE, SCS_HEURISTIC, ... */
+  uint32_t kl_heuristic;/* greedy incumbent */
+  uint32_t h_size;      /* vertices written to the community buffer */
+  uint32_t h_verified;  /* 1: community connected, contains q, size within
+                           [l,h] and min degree == degree */
+  uint64_t nodes;       /* search tasks processed */
+  uint64_t latency_ns;  /* submit -> result available */
+  uint64_t search_ns;   /* device search time (admission -> finish) */
+} scs_result;
+
+typedef struct scs_engine scs_engine;
+
+/* Create from an edge-list file in the reference format: a "<n> <m>" header
+ * then "u v" pairs (src/Graph.h:5-67).  Self-loops dropped, duplicates
+ * merged. */
+int scs_create(scs_engine **out, const char *edge_list_path,
+               const scs_config *cfg);
+
+/* Create from a symmetric CSR with ascending neighbour lists. */
+int scs_create_csr(scs_engine **out, uint32_t n, const uint32_t *off,
+                   const uint32_t *adj, const scs_config *cfg);
+
+/* Graph facts: n, directed adjacency entries, max degree. */
+int scs_graph_info(scs_engine *e, uint32_t *n, uint64_t *nnz, uint32_t *dmax);
+
+/* Copy core numbers (n entries) computed at creation. */
+int scs_core_numbers(scs_engine *e, uint32_t *core_out);
+
+/* Queue a query; returns a ticket.  Admission into a slot happens inside
+ * scs_run/scs_step as slots free up (continuous batching). */
+int scs_submit(scs_engine *e, const scs_query *q, uint64_t *ticket);
+
+/* Advance the engine: admit waiting queries into free slots, run one search
+ * slice, collect finished queries.  Returns the number of queries still
+ * outstanding (queued + running), or a negative error. */
+int scs_step(scs_engine *e);
+
+/* Run until every submitted query has a result. */
+int scs_run(scs_engine *e);
+
+/* Drain up to max finished results.  For result i the community's global
+ * vertex ids go to h_buf[i*h_stride ... i*h_stride + h_size) when h_buf is
+ * not NULL (h_stride >= the query's h).  Returns the count written. */
+int scs_poll(scs_engine *e, scs_result *out, int max, uint32_t *h_buf,
+             uint32_t h_stride);
+
+/* Engine counters (array of SCS_STAT_COUNT u64). */
+#define SCS_STAT_COUNT 16
+enum {
+  SCS_STAT_NODES = 0,     /* tasks processed */
+  SCS_STAT_SLICES = 1,    /* search slices launched */
+  SCS_STAT_DONATIONS = 2, /* tasks moved into the shared pool */
+  SCS_STAT_STEALS = 3,    /* tasks taken from the shared pool */
+  SCS_STAT_SPILLS = 4,    /* stack overflows spilled to the pool */
+  SCS_STAT_BYTES = 5,     /* algorithmic bytes moved by the search */
+  SCS_STAT_PREP_BYTES = 6,/* algorithmic bytes moved by preprocessing */
+  SCS_STAT_SEARCH_NS = 7, /* device time inside search slices */
+  SCS_STAT_PREP_NS = 8,   /* device time inside preprocessing */
+  SCS_STAT_LAUNCHES = 9   /* kernel launches issued */
+};
+int scs_stats(scs_engine *e, uint64_t *out);
+
+/* Text of the last error on this engine (or the last creation failure). */
+const char *scs_last_error(scs_engine *e);
+
+int scs_destroy(scs_engine *e);
+
+/* ---- host-only utilities (no GPU needed) ---- */
+
+/* Edge-list load (src/Graph.h:5-67) into a CSR allocated with malloc; free
+ * both arrays with scs_free. */
+int scs_read_edge_list(const char *path, uint32_t *n, uint64_t *nnz,
+                       uint32_t **off, uint32_t **adj);
+void scs_free(void *p);
+
+/* Core numbers (src/Graph.h:82-109). */
+int scs_core_decompose(uint32_t n, const uint32_t *off, const uint32_t *adj,
+                       uint32_t *core);
+
+/* Greedy incumbent kl = max(heu2, heu3, heu4) and its community
+ * (CSSC_heu, inc/heuristic.h:321-349).  H needs room for max(h, deg(q)+1). */
+int scs_greedy_incumbent(uint32_t n, const uint32_t *off, const uint32_t *adj,
+                         uint32_t l, uint32_t h, uint32_t q, uint32_t *kl,
+                         uint32_t *H, uint32_t *hsize);
+
+/* Distance bound ubD from n(k, D) (main.cu:154-172). */
+uint32_t scs_distance_bound(uint32_t kl, uint32_t h);
+
+/* ---- test hooks (used by the parity tests; no reference counterpart) ----
+ * These expose single stages of the pipeline so they can be compared with
+ * the CPU oracle.  They need an idle engine (no queries running). */
+
+/* Build the local (filtered) graphs of nq queries into slots 0..nq-1 with the
+ * given incumbents kl[i] and distance bounds ubd[i]; the stage restated from
+ * initialReductionRules/CompressTask/NeighborUpdate (src/helpers.cc:207-368).
+ * Writes each slot's local vertex count and local id of q. */
+int scs_debug_prepare(scs_engine *e, uint32_t nq, const scs_query *queries,
+                      const uint32_t *kl, const uint32_t *ubd,
+                      uint32_t *n_local, uint32_t *q_local);
+
+/* Copy a prepared slot's local graph: local->global ids, CSR without the
+ * row padding, and full-graph hop distances.  Any pointer may be NULL. */
+int scs_debug_local_graph(scs_engine *e, uint32_t slot, uint32_t *gid,
+                          uint32_t *off, uint32_t *adj, uint32_t *dist);
+
+/* Run ONE deterministic branch-and-bound step per task on the GPU with the
+ * search kernel's own step code (ProcessTask + FindDoms + Expand,
+ * src/helpers.cc:371-857).  Task t lives in slot task_slot[t], has incumbent
+ * kl_in[t] and entries (local_id<<1)|inC at task_entries[task_off[t] ..
+ * + task_len[t]), ascending.  Per task: out_hdr[16*t] gets the step header
+ * (same layout as the CPU oracle's orc_step), out_doms the kept dominated
+ * vertices, out_kids the children [s, csize, entries(s), degrees(s)] in the
+ * order Include, Dom_0.., Exclude, out_wit the witness C (count at index
+ * 512).  Strides: doms >= 15, wit >= 513. */
+int scs_debug_step(scs_engine *e, uint32_t ntasks, const uint32_t *task_slot,
+                   const uint32_t *kl_in, const uint64_t *task_off,
+                   const uint32_t *task_len, const uint32_t *task_entries,
+                   uint32_t *out_hdr, uint32_t *out_doms, uint32_t doms_stride,
+                   uint32_t *out_kids, uint64_t kids_stride, uint32_t *out_wit,
+                   uint32_t wit_stride);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

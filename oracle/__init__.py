@@ -208,3 +208,93 @@ class RefLib:
         hs = C.c_uint32()
         kl = self.L.ref_heu(which, l, h, q, _p(H), C.byref(hs))
         return int(kl), H[: hs.value].copy()
+
+
+class OracleCtx:
+    """Per-query local graph (orc_prepare) plus single steps (orc_step)."""
+
+    def __init__(self, og, l, h, q, kl, ubd, limit_doms=10, rules=ALL_RULES,
+                 component_only=1):
+        self.ctx = QCtx()
+        nk = C.c_uint32()
+        lib().orc_prepare(C.byref(og.g), q, kl, ubd, component_only, C.byref(self.ctx), C.byref(nk))
+        self.ctx.l, self.ctx.h = l, h
+        self.ctx.limit_doms = limit_doms
+        self.ctx.dmax = og.dmax
+        self.ctx.rules = rules
+        self.n_kept = nk.value
+        n = self.ctx.n
+        self.n = n
+        self.q_local = self.ctx.q_local
+        self.off = np.ctypeslib.as_array(self.ctx.off, shape=(n + 1,)).copy()
+        e = int(self.off[-1])
+        self.adj = np.ctypeslib.as_array(self.ctx.adj, shape=(max(e, 1),))[:e].copy()
+        self.gid = np.ctypeslib.as_array(self.ctx.gid, shape=(max(n, 1),))[:n].copy()
+        self.dist = np.ctypeslib.as_array(self.ctx.dist, shape=(max(n, 1),))[:n].copy()
+
+    def root(self):
+        return np.array([(i << 1) | (1 if i == self.q_local else 0) for i in range(self.n)],
+                        dtype=np.uint32)
+
+    def step(self, entries, kl):
+        entries = np.ascontiguousarray(entries, dtype=np.uint32)
+        s = len(entries)
+        hdr = np.zeros(16, dtype=np.uint32)
+        doms = np.zeros(max(self.ctx.limit_doms, 1) + 1, dtype=np.uint32)
+        cap = (s + 2) * (self.ctx.limit_doms + 2) + 8
+        kids = np.zeros(cap, dtype=np.uint32)
+        wit = np.zeros(s + 1, dtype=np.uint32)
+        rc = lib().orc_step(C.byref(self.ctx), _p(entries), s, kl, _p(hdr), _p(doms),
+                            _p(kids), cap, _p(wit))
+        assert rc == 0
+        children = []
+        w = 0
+        if hdr[0] == 0:
+            for _ in range(int(hdr[9])):
+                s2, c2 = int(kids[w]), int(kids[w + 1])
+                children.append((s2, c2, kids[w + 2: w + 2 + s2].copy()))
+                w += 2 + s2
+        return dict(hdr=hdr, doms=doms[: int(hdr[8])].copy(), kids=children,
+                    wit=np.sort(wit[: int(hdr[11])].copy()) if hdr[2] != 0xFFFFFFFF else None)
+
+    def degrees(self, entries):
+        """(dC, dR) of each entry inside the task (reference semantics of
+        degreeInC/degreeInR, inc/Intialize.h:120-138)."""
+        ids = entries >> 1
+        inC = (entries & 1).astype(bool)
+        pos = {int(v): i for i, v in enumerate(ids)}
+        dc = np.zeros(len(ids), dtype=np.uint32)
+        dr = np.zeros(len(ids), dtype=np.uint32)
+        for i, v in enumerate(ids.tolist()):
+            for w in self.adj[self.off[v]:self.off[v + 1]].tolist():
+                j = pos.get(w)
+                if j is not None:
+                    if inC[j]:
+                        dc[i] += 1
+                    else:
+                        dr[i] += 1
+        return dc, dr
+
+    def collect_tasks(self, kl, limit):
+        """Tasks of the serial depth-first search (Include first), with the
+        incumbent each was processed under: [(entries, kl), ...]."""
+        stack = [self.root()]
+        out = []
+        while stack and len(out) < limit:
+            e = stack.pop()
+            out.append((e, kl))
+            r = self.step(e, kl)
+            kl = int(r["hdr"][1])
+            for ch in reversed(r["kids"]):
+                stack.append(ch[2])
+        return out
+
+    def close(self):
+        if self.ctx.off:
+            lib().orc_qctx_free(C.byref(self.ctx))
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

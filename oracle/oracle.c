@@ -821,6 +821,7 @@ int orc_step(orc_qctx *ctx, const uint32_t *task, uint32_t s, uint32_t kl,
 done:
 #undef MINDEG_UPDATE
   hdr[1] = kl;
+  hdr[3] = csize;
   hdr[2] = best;
   for (uint32_t i = 0; i < s; i++) ctx->pos[v[i]] = -1;
   free(v);

@@ -1,0 +1,68 @@
+"""Build the engine library in-tree: scs_gb300/_lib/libscs.so (sm_103a).
+
+Each translation unit is compiled in parallel with nvcc (CUDA) or g++ (host
+C++), then linked into one shared library exporting include/scs.h.
+"""
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+OUT = os.path.join(HERE, "_lib")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+CU = ["prep.cu", "bnb.cu", "engine.cu"]
+CXX = ["host_graph.cpp", "host_api.cpp"]
+LIB = "libscs.so"
+
+
+def nvcc():
+    p = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(p):
+        raise RuntimeError("nvcc not found")
+    return p
+
+
+def _deps_mtime():
+    names = os.listdir(CSRC) + [os.path.join("..", "..", "include", "scs.h")]
+    return max(os.path.getmtime(os.path.join(CSRC, f)) for f in names)
+
+
+def lib_path():
+    return os.path.join(OUT, LIB)
+
+
+def build(verbose=False, force=False):
+    os.makedirs(OUT, exist_ok=True)
+    out = lib_path()
+    if not force and os.path.exists(out) and os.path.getmtime(out) >= _deps_mtime():
+        return out
+    objdir = os.path.join(OUT, "obj")
+    os.makedirs(objdir, exist_ok=True)
+    cmds = []
+    for f in CU:
+        cmds.append([nvcc(), *ARCH, "-O3", "-std=c++17", "-lineinfo",
+                     "-Xcompiler", "-fPIC", "-c", os.path.join(CSRC, f),
+                     "-o", os.path.join(objdir, f + ".o")])
+    for f in CXX:
+        cmds.append(["g++", "-O3", "-std=c++17", "-fPIC", "-Wall", "-c",
+                     os.path.join(CSRC, f), "-o", os.path.join(objdir, f + ".o")])
+
+    def run(cmd):
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("build failed: %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
+        return r.stderr
+
+    with cf.ThreadPoolExecutor(max_workers=len(cmds)) as ex:
+        list(ex.map(run, cmds))
+    objs = [os.path.join(objdir, f + ".o") for f in CU + CXX]
+    run([nvcc(), *ARCH, "-shared", "-o", out, *objs, "-lcudart", "-lpthread"])
+    return out
+
+
+if __name__ == "__main__":
+    print(build(verbose=True, force=True))

@@ -1,0 +1,1288 @@
+// bnb.cu -- branch-and-bound search, one CTA per task.
+//
+// One step on a task (C, R) restates the reference's per-task pipeline:
+//   ProcessTask       src/helpers.cc:371-542  (min degree + incumbent,
+//                     rule 3, rules 1/2, bounds P1/P2, ustar)
+//   calculateMinimumDegree :893-930, reductionRule3 :932-968,
+//   reductionRule1and2 :970-1028, calculateUpperBoundDegree :1030-1102,
+//   selectUstar :1104-1168, FindDoms :545-670, Expand/writeTasks/
+//   writeDomTasks :673-857, :1171-1391.
+// The step is deterministic and identical to the CPU oracle's orc_step
+// (rules 3 and 1/2 applied to a fixpoint in synchronous rounds, ties to the
+// lowest local id, dominance inside the task, sequential score sums in
+// ascending neighbour order).
+//
+// GB300 mapping: the per-vertex state word (status | dC | dR) of the task's
+// query lives in shared memory, indexed by local vertex id; task records carry
+// dC/dR so loading a task is one coalesced pass; adjacency rows are read
+// with 16-byte loads; children are derived from the adjacency of u* and the
+// dominated vertices only; the Include child continues in place (depth-first
+// dive), the others go to the CTA's own LIFO stack in HBM, and the oldest
+// stack entry is donated to a shared pool when other CTAs are idle.  Every
+// spin-wait has an iteration bound and reports through Counters::error.
+#include "scs_device.cuh"
+
+namespace scs {
+
+constexpr int BT = SEARCH_THREADS;
+constexpr int NWARP = BT / 32;
+
+struct Sh {
+  uint32_t slot, s, csize, n_local, l, h, ldoms, rules, kl, q_local, dmax;
+  uint32_t outcome;  // 0 branched, 1 size, 2 bound, 3 no ustar / small
+  uint32_t best;     // best min degree evaluated this step
+  uint32_t cnt[4];
+  uint32_t p1, p2, nR;
+  uint32_t ustar, us_idx;
+  uint32_t ndoms, ndom_cand;
+  uint32_t doms[MAX_DOMS];
+  uint32_t doms_idx[MAX_DOMS];
+  uint32_t wit_pending;
+  uint32_t bt;
+  int have;
+  int stop;
+  unsigned long long rec;
+  uint32_t red_u[NWARP];
+  uint32_t red_u2[NWARP];
+  double red_d[NWARP];
+  uint32_t cl[CL_CAP];
+  uint32_t A[CL_CAP];
+  uint32_t B[CL_CAP];
+  uint32_t hist[CL_CAP + 1];
+  double wsum[NWARP][32];
+  uint32_t kid_len[MAX_DOMS + 2];
+  unsigned long long kid_dst[MAX_DOMS + 2];
+};
+
+__device__ __forceinline__ uint32_t st_of(uint32_t w) { return w >> 30; }
+__device__ __forceinline__ uint32_t dc_of(uint32_t w) { return (w >> 15) & DMASK; }
+__device__ __forceinline__ uint32_t dr_of(uint32_t w) { return w & DMASK; }
+__device__ __forceinline__ bool live(uint32_t w) {
+  uint32_t s = w >> 30;
+  return s == ST_R || s == ST_C;
+}
+
+__device__ __forceinline__ unsigned long long gtimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ uint32_t warp_min(uint32_t v) {
+#pragma unroll
+  for (int o = 16; o; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+__device__ __forceinline__ uint32_t warp_sum(uint32_t v) {
+#pragma unroll
+  for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ uint32_t block_min(uint32_t v, Sh &sh) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  v = warp_min(v);
+  if (lane == 0) sh.red_u[wid] = v;
+  __syncthreads();
+  uint32_t r = UINT32_MAX;
+  for (int i = 0; i < NWARP; i++) r = min(r, sh.red_u[i]);
+  __syncthreads();
+  return r;
+}
+
+__device__ uint32_t block_sum(uint32_t v, Sh &sh) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  v = warp_sum(v);
+  if (lane == 0) sh.red_u[wid] = v;
+  __syncthreads();
+  uint32_t r = 0;
+  for (int i = 0; i < NWARP; i++) r += sh.red_u[i];
+  __syncthreads();
+  return r;
+}
+
+// max score, ties to the smaller id; returns via sh.red_d[0]/sh.red_u[0]
+__device__ void block_argmax(double sc, uint32_t id, Sh &sh, double &osc,
+                             uint32_t &oid) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o; o >>= 1) {
+    double s2 = __shfl_xor_sync(0xffffffffu, sc, o);
+    uint32_t i2 = __shfl_xor_sync(0xffffffffu, id, o);
+    if (s2 > sc || (s2 == sc && i2 < id)) {
+      sc = s2;
+      id = i2;
+    }
+  }
+  if (lane == 0) {
+    sh.red_d[wid] = sc;
+    sh.red_u2[wid] = id;
+  }
+  __syncthreads();
+  double bs = sh.red_d[0];
+  uint32_t bi = sh.red_u2[0];
+  for (int i = 1; i < NWARP; i++) {
+    double s2 = sh.red_d[i];
+    uint32_t i2 = sh.red_u2[i];
+    if (s2 > bs || (s2 == bs && i2 < bi)) {
+      bs = s2;
+      bi = i2;
+    }
+  }
+  __syncthreads();
+  osc = bs;
+  oid = bi;
+}
+
+// Append `want` lanes' values to tmp[] with a shared counter.
+__device__ __forceinline__ void warp_append(bool want, uint32_t val,
+                                            uint32_t *cnt, uint32_t *dst) {
+  const int lane = threadIdx.x & 31;
+  unsigned m = __ballot_sync(0xffffffffu, want);
+  if (!m) return;
+  uint32_t base = 0;
+  if (lane == __ffs(m) - 1) base = atomicAdd(cnt, __popc(m));
+  base = __shfl_sync(0xffffffffu, base, __ffs(m) - 1);
+  if (want) dst[base + __popc(m & ((1u << lane) - 1u))] = val;
+}
+
+struct Task {
+  uint32_t *W;
+  uint32_t *list;
+  uint32_t *aux;
+  uint32_t *tmp;
+  double *dsc;
+  const uint32_t *off;
+  const uint32_t *adj;
+  const uint16_t *dist;
+  const uint32_t *gid;
+  uint32_t *witness;
+  Slot *slot;
+};
+
+// ---------------------------------------------------------------------------
+// load a record into the state words / live list / C list
+// ---------------------------------------------------------------------------
+__device__ void load_record(const uint32_t *rec, Task &T, Sh &sh) {
+  const int t = threadIdx.x;
+  const uint32_t s = sh.s;
+  const uint32_t *ent = rec + REC_HDR;
+  const uint32_t *deg = rec + REC_HDR + s;
+  if (t == 0) sh.cnt[0] = 0;
+  __syncthreads();
+  for (uint32_t i = t; i < s; i += BT) {
+    uint32_t e = ent[i], dg = deg[i];
+    uint32_t id = e >> 1, c = e & 1u;
+    T.W[id] = ((c ? ST_C : ST_R) << 30) | ((dg >> 16) << 15) | (dg & 0xFFFFu);
+    T.list[i] = id;
+    if (c) {
+      uint32_t k = atomicAdd(&sh.cnt[0], 1u);
+      if (k < CL_CAP) sh.cl[k] = id;
+    }
+  }
+  __syncthreads();
+}
+
+__device__ void clear_state(Task &T, Sh &sh) {
+  for (uint32_t i = threadIdx.x; i < sh.s; i += BT) T.W[T.list[i]] = 0;
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// minimum degree of C and incumbent update (src/helpers.cc:446-455)
+// ---------------------------------------------------------------------------
+__device__ void eval_mindeg(Task &T, Sh &sh, bool test, uint32_t *t_wit) {
+  const int t = threadIdx.x;
+  const uint32_t cs = sh.csize;
+  uint32_t v = UINT32_MAX;
+  for (uint32_t i = t; i < cs && i < CL_CAP; i += BT) v = min(v, dc_of(T.W[sh.cl[i]]));
+  uint32_t md = block_min(v, sh);
+  if (md == UINT32_MAX) return;
+  bool improve_step = (sh.best == UINT32_MAX || md > sh.best);
+  if (improve_step && t == 0) sh.best = md;
+  if (md > sh.kl && t == 0) sh.kl = md;
+  if (test) {
+    if (improve_step) {
+      for (uint32_t i = t; i < cs; i += BT) t_wit[i] = sh.cl[i];
+      if (t == 0) t_wit[CL_CAP] = cs;  // count stored past the list
+    }
+    __syncthreads();
+    return;
+  }
+  // global incumbent + witness (bounded lock)
+  if (t == 0) {
+    uint32_t old = atomicMax(&T.slot->kl, md);
+    sh.wit_pending = 0;
+    if (old < md) {
+      uint32_t spins = 0;
+      while (atomicCAS(&T.slot->wit_lock, 0u, 1u) != 0u) {
+        if (++spins > (1u << 22)) break;
+        __nanosleep(64);
+      }
+      if (spins <= (1u << 22)) {
+        if (*(volatile uint32_t *)&T.slot->wit_val < md + 1u)
+          sh.wit_pending = 1;
+        else
+          atomicExch(&T.slot->wit_lock, 0u);
+      }
+    }
+  }
+  __syncthreads();
+  if (sh.wit_pending) {
+    for (uint32_t i = t; i < cs && i < CL_CAP; i += BT) T.witness[i] = T.gid[sh.cl[i]];
+    __threadfence();
+    __syncthreads();
+    if (t == 0) {
+      T.slot->wit_n = min(cs, (uint32_t)CL_CAP);
+      T.slot->wit_val = md + 1u;  // stored +1 so that 0 means none
+      __threadfence();
+      atomicExch(&T.slot->wit_lock, 0u);
+    }
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ void refresh_kl(Task &T, Sh &sh, bool test) {
+  if (!test && threadIdx.x == 0) {
+    uint32_t g = *(volatile uint32_t *)&T.slot->kl;
+    if (g > sh.kl) sh.kl = g;
+  }
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// rule 3 to a fixpoint: every R neighbour of a C vertex with dC+dR == kl+1
+// moves to C (src/helpers.cc:932-968)
+// ---------------------------------------------------------------------------
+__device__ void rule3(Task &T, Sh &sh) {
+  const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+  for (;;) {
+    if (t == 0) sh.cnt[2] = 0;
+    __syncthreads();
+    const uint32_t kl = sh.kl, cs = min(sh.csize, (uint32_t)CL_CAP);
+    for (uint32_t ci = wid; ci < cs; ci += NWARP) {
+      uint32_t u = sh.cl[ci];
+      uint32_t wu = T.W[u];
+      if (dc_of(wu) + dr_of(wu) != kl + 1u || dr_of(wu) == 0) continue;
+      uint32_t b = T.off[u], e = T.off[u + 1];
+      for (uint32_t k = b; k < e; k += 32) {
+        bool want = false;
+        uint32_t nb = SENT;
+        if (k + lane < e) {
+          nb = T.adj[k + lane];
+          if (nb != SENT && st_of(T.W[nb]) == ST_R)
+            want = atomicExch(&T.aux[nb], 1u) == 0u;
+        }
+        warp_append(want, nb, &sh.cnt[2], T.tmp);
+      }
+    }
+    __syncthreads();
+    const uint32_t np = sh.cnt[2];
+    if (np == 0) break;
+    for (uint32_t i = t; i < np; i += BT) {
+      uint32_t x = T.tmp[i];
+      T.aux[x] = 0;
+      T.W[x] += ST_ONE;  // R -> C
+      uint32_t k = sh.csize + i;
+      if (k < CL_CAP) sh.cl[k] = x;
+    }
+    __syncthreads();
+    if (t == 0) sh.csize += np;
+    for (uint32_t pi = wid; pi < np; pi += NWARP) {
+      uint32_t x = T.tmp[pi];
+      uint32_t b = T.off[x], e = T.off[x + 1];
+      for (uint32_t k = b + lane; k < e; k += 32) {
+        uint32_t nb = T.adj[k];
+        if (nb != SENT && live(T.W[nb])) atomicAdd(&T.W[nb], DC_ONE - 1u);
+      }
+    }
+    __syncthreads();
+    if (sh.csize > sh.h) break;
+  }
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// rules 1/2 to a fixpoint (src/helpers.cc:970-1028), then compact the list
+// ---------------------------------------------------------------------------
+__device__ void rule12(Task &T, Sh &sh, bool test) {
+  const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+  const uint32_t h = sh.h, rules = sh.rules;
+  if (rules & (R_RED1 | R_RED2)) {
+    for (;;) {
+      refresh_kl(T, sh, test);
+      const uint32_t kl = sh.kl, cs = sh.csize, s = sh.s;
+      const uint32_t ubd = ubd_dev(kl, h);
+      if (t == 0) sh.cnt[1] = 0;
+      __syncthreads();
+      for (uint32_t i0 = 0; i0 < s; i0 += BT) {
+        uint32_t i = i0 + t;
+        bool rm = false;
+        uint32_t x = 0;
+        if (i < s) {
+          x = T.list[i];
+          uint32_t w = T.W[x];
+          if (st_of(w) == ST_R) {
+            uint32_t dc = dc_of(w), dr = dr_of(w);
+            if (rules & R_RED1) {
+              uint32_t a = dr + dc, b2 = dc + h - cs - 1u;
+              if (min(a, b2) <= kl) rm = true;
+            }
+            if ((rules & R_RED2) && (uint32_t)T.dist[x] > ubd) rm = true;
+          }
+        }
+        warp_append(rm, x, &sh.cnt[1], T.tmp);
+      }
+      __syncthreads();
+      const uint32_t nr = sh.cnt[1];
+      if (nr == 0) break;
+      for (uint32_t i = t; i < nr; i += BT) T.W[T.tmp[i]] = ST_X << 30;
+      __syncthreads();
+      for (uint32_t ri = wid; ri < nr; ri += NWARP) {
+        uint32_t x = T.tmp[ri];
+        uint32_t b = T.off[x], e = T.off[x + 1];
+        for (uint32_t k = b + lane; k < e; k += 32) {
+          uint32_t nb = T.adj[k];
+          if (nb != SENT && live(T.W[nb])) atomicSub(&T.W[nb], 1u);
+        }
+      }
+      __syncthreads();
+    }
+  }
+  // compact: drop removed entries, count R
+  const uint32_t s = sh.s;
+  uint32_t out = 0, nR = 0;
+  for (uint32_t i0 = 0; i0 < s; i0 += BT) {
+    uint32_t i = i0 + t;
+    uint32_t x = 0, w = 0;
+    bool keep = false;
+    if (i < s) {
+      x = T.list[i];
+      w = T.W[x];
+      keep = st_of(w) != ST_X;
+      if (!keep) T.W[x] = 0;
+      if (keep && st_of(w) == ST_R) nR++;
+    }
+    unsigned m = __ballot_sync(0xffffffffu, keep);
+    if (lane == 0) sh.red_u[wid] = __popc(m);
+    __syncthreads();
+    uint32_t before = 0, tot = 0;
+    for (int k = 0; k < NWARP; k++) {
+      uint32_t c = sh.red_u[k];
+      if (k < wid) before += c;
+      tot += c;
+    }
+    __syncthreads();
+    if (keep) T.list[out + before + __popc(m & ((1u << lane) - 1u))] = x;
+    out += tot;
+    __syncthreads();
+  }
+  nR = block_sum(nR, sh);
+  if (t == 0) {
+    sh.s = out;
+    sh.nR = nR;
+  }
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// bounds P1/P2 (src/helpers.cc:1030-1102)
+// ---------------------------------------------------------------------------
+__device__ void bounds(Task &T, Sh &sh) {
+  const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+  const uint32_t cs = min(sh.csize, (uint32_t)CL_CAP), h = sh.h;
+  uint32_t p1 = UINT32_MAX;
+  if (sh.rules & R_PRUN1) {
+    for (uint32_t i = t; i < cs; i += BT) {
+      uint32_t w = T.W[sh.cl[i]];
+      uint32_t a = dc_of(w) + h - sh.csize, b = dr_of(w) + dc_of(w);
+      p1 = min(p1, min(a, b));
+    }
+    p1 = block_min(p1, sh);
+  }
+  uint32_t p2 = UINT32_MAX;
+  if (sh.rules & R_PRUN2) {
+    for (uint32_t i = t; i <= cs; i += BT) sh.hist[i] = 0;
+    __syncthreads();
+    for (uint32_t i = t; i < sh.s; i += BT) {
+      uint32_t w = T.W[T.list[i]];
+      if (st_of(w) == ST_R) atomicAdd(&sh.hist[min(dc_of(w), cs)], 1u);
+    }
+    // rank sort of C degrees into A (ascending)
+    for (uint32_t i = t; i < cs; i += BT) {
+      uint32_t vi = dc_of(T.W[sh.cl[i]]), r = 0;
+      for (uint32_t j = 0; j < cs; j++) {
+        uint32_t vj = dc_of(T.W[sh.cl[j]]);
+        r += (vj < vi) || (vj == vi && j < i);
+      }
+      sh.A[r] = vi;
+    }
+    __syncthreads();
+    if (t == 0) {  // B: the top min(h-|C|, |R|) R degrees, descending
+      uint32_t want = min(h - sh.csize, sh.nR), nb = 0;
+      for (int v = (int)cs; v >= 0 && nb < want; v--) {
+        uint32_t c = sh.hist[v];
+        while (c-- && nb < want) sh.B[nb++] = (uint32_t)v;
+      }
+      sh.cnt[3] = nb;
+    }
+    __syncthreads();
+    if (wid == 0) {
+      const uint32_t nb = sh.cnt[3];
+      for (uint32_t it = 0; it < nb; it++) {
+        uint32_t k = min(sh.B[it], cs);
+        if (k == 0) break;
+        uint32_t v = sh.A[k - 1];
+        uint32_t lt = 0, le = 0;
+        for (uint32_t i = lane; i < cs; i += 32) {
+          uint32_t a = sh.A[i];
+          lt += a < v;
+          le += a <= v;
+        }
+        lt = warp_sum(lt);
+        le = warp_sum(le);
+        __syncwarp();
+        uint32_t bcount = k - lt, c = le - lt;
+        for (uint32_t i = lane; i < cs; i += 32) {
+          if (i < lt) sh.A[i] += 1u;
+          else if (i < lt + c - bcount) sh.A[i] = v;
+          else if (i < le) sh.A[i] = v + 1u;
+        }
+        __syncwarp();
+      }
+    }
+    __syncthreads();
+    p2 = cs ? sh.A[0] : UINT32_MAX;
+  }
+  if (t == 0) {
+    sh.p1 = p1;
+    sh.p2 = p2;
+  }
+  __syncthreads();
+}
+
+// ordered sum of 1/dC over C neighbours of x (ascending neighbour order);
+// zero_dc_weight: term used when dC == 0 (1.0 for ustar, 0.0 for doms).
+// When `dom_check`, also tests that every live neighbour is marked in aux.
+__device__ double warp_score(Task &T, Sh &sh, uint32_t x, double zero_w,
+                             bool dom_check, bool &dominated) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  double total = 0.0;
+  dominated = true;
+  uint32_t b = T.off[x], e = T.off[x + 1];
+  for (uint32_t k = b; k < e; k += 32) {
+    double term = 0.0;
+    bool bad = false;
+    if (k + lane < e) {
+      uint32_t nb = T.adj[k + lane];
+      if (nb != SENT) {
+        uint32_t w = T.W[nb];
+        if (dom_check && live(w) && T.aux[nb] == 0u) bad = true;
+        if (st_of(w) == ST_C) {
+          uint32_t dc = dc_of(w);
+          term = dc ? __ddiv_rn(1.0, (double)dc) : zero_w;
+        }
+      }
+    }
+    if (dom_check && __any_sync(0xffffffffu, bad)) {
+      dominated = false;
+      return 0.0;
+    }
+    unsigned m = __ballot_sync(0xffffffffu, term != 0.0);
+    if (m) {
+      if (term != 0.0) sh.wsum[wid][__popc(m & ((1u << lane) - 1u))] = term;
+      __syncwarp();
+      if (lane == 0) {
+        int c = __popc(m);
+        for (int j = 0; j < c; j++) total = __dadd_rn(total, sh.wsum[wid][j]);
+      }
+      __syncwarp();
+    }
+  }
+  return __shfl_sync(0xffffffffu, total, 0);
+}
+
+// ---------------------------------------------------------------------------
+// ustar (src/helpers.cc:1104-1168) and dominated vertices (:545-670)
+// ---------------------------------------------------------------------------
+__device__ void choose_ustar(Task &T, Sh &sh) {
+  const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+  const uint32_t s = sh.s;
+  if (t == 0) sh.cnt[0] = 0;
+  __syncthreads();
+  for (uint32_t i0 = 0; i0 < s; i0 += BT) {
+    uint32_t i = i0 + t;
+    bool c = false;
+    uint32_t x = 0;
+    if (i < s) {
+      x = T.list[i];
+      uint32_t w = T.W[x];
+      c = st_of(w) == ST_R && dc_of(w) > 0;
+    }
+    warp_append(c, x, &sh.cnt[0], T.tmp);
+  }
+  __syncthreads();
+  const uint32_t nc = sh.cnt[0];
+  const double dmax = (double)sh.dmax;
+  double best = 0.0;
+  uint32_t bid = UINT32_MAX;
+  for (uint32_t ci = wid; ci < nc; ci += NWARP) {
+    uint32_t x = T.tmp[ci];
+    bool dummy;
+    double sc = warp_score(T, sh, x, 1.0, false, dummy);
+    if (sc > 0.0) sc = __dadd_rn(sc, __ddiv_rn((double)dr_of(T.W[x]), dmax));
+    if (sc > best || (sc == best && sc > 0.0 && x < bid)) {
+      best = sc;
+      bid = x;
+    }
+  }
+  if (lane != 0) {
+    best = 0.0;
+    bid = UINT32_MAX;
+  }
+  double osc;
+  uint32_t oid;
+  block_argmax(best, bid, sh, osc, oid);
+  if (t == 0) {
+    sh.ustar = (osc > 0.0) ? oid : UINT32_MAX;
+    sh.ndom_cand = nc;
+  }
+  __syncthreads();
+}
+
+__device__ uint32_t list_index(const uint32_t *list, uint32_t s, uint32_t x) {
+  uint32_t lo = 0, hi = s;
+  while (lo < hi) {
+    uint32_t mid = (lo + hi) >> 1;
+    if (list[mid] < x) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+__device__ void find_doms(Task &T, Sh &sh) {
+  const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+  const uint32_t u = sh.ustar;
+  if (t == 0) {
+    sh.ndoms = 0;
+    sh.cnt[1] = 0;
+  }
+  __syncthreads();
+  if (sh.ldoms == 0) return;
+  // mark N_T(u*) and u*
+  {
+    uint32_t b = T.off[u], e = T.off[u + 1];
+    for (uint32_t k = b + t; k < e; k += BT) {
+      uint32_t nb = T.adj[k];
+      if (nb != SENT && live(T.W[nb])) T.aux[nb] = 1u;
+    }
+    if (t == 0) T.aux[u] = 1u;
+  }
+  __syncthreads();
+  // candidates were collected by choose_ustar in tmp[0..nc): R with dC > 0
+  const uint32_t nc = sh.ndom_cand;
+  const double dmax = (double)sh.dmax;
+  uint32_t *dom_id = T.tmp + sh.s;  // second half of tmp (s <= n)
+  for (uint32_t ci = wid; ci < nc; ci += NWARP) {
+    uint32_t x = T.tmp[ci];
+    if (x == u) continue;
+    bool dom;
+    double sc = warp_score(T, sh, x, 0.0, true, dom);
+    if (dom) {
+      sc = __dadd_rn(sc, __ddiv_rn((double)dr_of(T.W[x]), dmax));
+      if (lane == 0) {
+        uint32_t k = atomicAdd(&sh.cnt[1], 1u);
+        dom_id[k] = x;
+        T.dsc[k] = sc;
+      }
+    }
+  }
+  __syncthreads();
+  // clear marks
+  {
+    uint32_t b = T.off[u], e = T.off[u + 1];
+    for (uint32_t k = b + t; k < e; k += BT) {
+      uint32_t nb = T.adj[k];
+      if (nb != SENT) T.aux[nb] = 0u;
+    }
+    if (t == 0) T.aux[u] = 0u;
+  }
+  __syncthreads();
+  const uint32_t nd = sh.cnt[1];
+  const uint32_t k = min(nd, min(sh.ldoms, (uint32_t)MAX_DOMS));
+  for (uint32_t r = 0; r < k; r++) {
+    double bs = -1.0;
+    uint32_t bi = UINT32_MAX, bpos = UINT32_MAX;
+    for (uint32_t i = t; i < nd; i += BT) {
+      double sc = T.dsc[i];
+      uint32_t x = dom_id[i];
+      if (sc > bs || (sc == bs && x < bi)) {
+        bs = sc;
+        bi = x;
+        bpos = i;
+      }
+    }
+    double osc;
+    uint32_t oid;
+    block_argmax(bs, bi, sh, osc, oid);
+    if (bi == oid && bpos != UINT32_MAX && bs == osc) {
+      T.dsc[bpos] = -2.0;  // exclude from later rounds
+      sh.doms[r] = oid;
+    }
+    __syncthreads();
+  }
+  if (t == 0) sh.ndoms = k;
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// children.  aux[x] bit 0: x ~ u*, bit j+1: x ~ d_j; bits 16..20: rank+1 if
+// x == d_rank; bit 21: x == u*.
+// child code: 0 = Include, 1..k = Dom_{code-1}, k+1 = Exclude
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool child_skip(uint32_t a, uint32_t code,
+                                           uint32_t k) {
+  uint32_t rk = (a >> 16) & 31u;  // rank + 1 (0: not a dom)
+  bool is_u = (a >> 21) & 1u;
+  if (code == k + 1) return is_u || rk;           // Exclude drops u*, D
+  if (code == 0) return rk != 0;                  // Include drops D
+  return rk != 0 && rk < code;                    // Dom_i drops d_0..d_{i-1}
+}
+
+__device__ __forceinline__ void child_entry(uint32_t x, uint32_t w, uint32_t a,
+                                            uint32_t code, uint32_t k,
+                                            uint32_t &ent, uint32_t &deg) {
+  uint32_t rk = (a >> 16) & 31u;
+  bool is_u = (a >> 21) & 1u;
+  uint32_t dc = dc_of(w), dr = dr_of(w);
+  bool inC = st_of(w) == ST_C;
+  uint32_t adj_u = a & 1u;
+  uint32_t domadj = (a >> 1) & ((1u << k) - 1u);
+  if (code == k + 1) {           // Exclude: u*, D removed
+    dr -= adj_u + __popc(domadj);
+  } else if (code == 0) {        // Include: u* -> C, D removed
+    dc += adj_u;
+    dr -= adj_u + __popc(domadj);
+    inC = inC || is_u;
+  } else {                       // Dom_i: u*, d_i -> C; d_0..d_{i-1} removed
+    uint32_t i = code - 1;
+    uint32_t adj_i = (domadj >> i) & 1u;
+    uint32_t lower = domadj & ((1u << i) - 1u);
+    dc += adj_u + adj_i;
+    dr -= adj_u + adj_i + __popc(lower);
+    inC = inC || is_u || (rk == i + 1);
+  }
+  ent = (x << 1) | (inC ? 1u : 0u);
+  deg = (dc << 16) | dr;
+}
+
+__device__ void mark_children(Task &T, Sh &sh) {
+  const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+  const uint32_t k = sh.ndoms;
+  // adjacency bits: warp per marked vertex
+  for (uint32_t j = wid; j <= k; j += NWARP) {
+    uint32_t v = j == 0 ? sh.ustar : sh.doms[j - 1];
+    uint32_t b = T.off[v], e = T.off[v + 1];
+    for (uint32_t q = b + lane; q < e; q += 32) {
+      uint32_t nb = T.adj[q];
+      if (nb != SENT && live(T.W[nb])) atomicOr(&T.aux[nb], 1u << j);
+    }
+  }
+  __syncthreads();
+  if (t == 0) {
+    atomicOr(&T.aux[sh.ustar], 1u << 21);
+    sh.us_idx = list_index(T.list, sh.s, sh.ustar);
+  }
+  if (t < k) {
+    atomicOr(&T.aux[sh.doms[t]], (t + 1u) << 16);
+    sh.doms_idx[t] = list_index(T.list, sh.s, sh.doms[t]);
+  }
+  __syncthreads();
+}
+
+// number of skipped list entries before index i for a child
+__device__ __forceinline__ uint32_t skipped_before(const Sh &sh, uint32_t i,
+                                                   uint32_t code) {
+  const uint32_t k = sh.ndoms;
+  uint32_t c = 0;
+  if (code == k + 1 && sh.us_idx < i) c++;
+  for (uint32_t j = 0; j < k; j++) {
+    bool sk = (code == 0 || code == k + 1) ? true : (j + 1 < code);
+    if (sk && sh.doms_idx[j] < i) c++;
+  }
+  return c;
+}
+
+__device__ __forceinline__ void child_shape(const Sh &sh, uint32_t code,
+                                            uint32_t &s2, uint32_t &c2) {
+  const uint32_t k = sh.ndoms;
+  if (code == 0) {
+    s2 = sh.s - k;
+    c2 = sh.csize + 1;
+  } else if (code == k + 1) {
+    s2 = sh.s - 1 - k;
+    c2 = sh.csize;
+  } else {
+    s2 = sh.s - (code - 1);
+    c2 = sh.csize + 2;
+  }
+}
+
+__device__ __forceinline__ bool child_alive(const Sh &sh, uint32_t s2,
+                                            uint32_t c2) {
+  return c2 <= sh.h && s2 >= sh.l;
+}
+
+// write child `code`: entries to ent[], degrees to deg[]; when rec is not
+// null also the record header and footer (ent == rec + REC_HDR, deg == ent+s2)
+__device__ void write_child(Task &T, Sh &sh, uint32_t code, uint32_t *ent_dst,
+                            uint32_t *deg_dst, uint32_t *rec) {
+  const int t = threadIdx.x;
+  uint32_t s2, c2;
+  child_shape(sh, code, s2, c2);
+  const uint32_t s = sh.s, k = sh.ndoms;
+  for (uint32_t i = t; i < s; i += BT) {
+    uint32_t x = T.list[i];
+    uint32_t a = T.aux[x];
+    if (child_skip(a, code, k)) continue;
+    uint32_t o = i - skipped_before(sh, i, code);
+    uint32_t ent, deg;
+    child_entry(x, T.W[x], a, code, k, ent, deg);
+    ent_dst[o] = ent;
+    deg_dst[o] = deg;
+  }
+  if (t == 0 && rec) {
+    rec[0] = sh.slot;
+    rec[1] = s2;
+    rec[2] = c2;
+    rec[3] = 2 * s2 + 5;
+    rec[REC_HDR + 2 * s2] = 2 * s2 + 5;
+  }
+}
+
+// apply the Include child to the in-CTA state (continue depth-first)
+__device__ void apply_include(Task &T, Sh &sh) {
+  const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+  const uint32_t s = sh.s, k = sh.ndoms;
+  for (uint32_t i = t; i < s; i += BT) {
+    uint32_t x = T.list[i];
+    uint32_t a = T.aux[x];
+    uint32_t rk = (a >> 16) & 31u;
+    if (rk) {
+      T.W[x] = 0;
+    } else {
+      uint32_t adj_u = a & 1u;
+      uint32_t domadj = (a >> 1) & ((1u << k) - 1u);
+      uint32_t w = T.W[x];
+      w += adj_u * DC_ONE;
+      w -= adj_u + __popc(domadj);
+      if ((a >> 21) & 1u) w += ST_ONE;
+      T.W[x] = w;
+    }
+    T.aux[x] = 0;
+  }
+  __syncthreads();
+  // compact the live list (drop D)
+  uint32_t out = 0;
+  for (uint32_t i0 = 0; i0 < s; i0 += BT) {
+    uint32_t i = i0 + t;
+    uint32_t x = 0;
+    bool keep = false;
+    if (i < s) {
+      x = T.list[i];
+      keep = T.W[x] != 0;
+    }
+    unsigned m = __ballot_sync(0xffffffffu, keep);
+    if (lane == 0) sh.red_u[wid] = __popc(m);
+    __syncthreads();
+    uint32_t before = 0, tot = 0;
+    for (int q = 0; q < NWARP; q++) {
+      uint32_t c = sh.red_u[q];
+      if (q < wid) before += c;
+      tot += c;
+    }
+    __syncthreads();
+    if (keep) T.list[out + before + __popc(m & ((1u << lane) - 1u))] = x;
+    out += tot;
+    __syncthreads();
+  }
+  if (t == 0) {
+    if (sh.csize < CL_CAP) sh.cl[sh.csize] = sh.ustar;
+    sh.csize += 1;
+    sh.s = out;
+  }
+  __syncthreads();
+}
+
+__device__ void clear_aux_list(Task &T, Sh &sh) {
+  for (uint32_t i = threadIdx.x; i < sh.s; i += BT) T.aux[T.list[i]] = 0;
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// one step on the loaded task (phases up to the choice of u* and doms)
+// returns outcome in sh.outcome
+// ---------------------------------------------------------------------------
+__device__ void step_core(Task &T, Sh &sh, bool test, uint32_t *t_wit) {
+  const int t = threadIdx.x;
+  if (t == 0) {
+    sh.best = UINT32_MAX;
+    sh.outcome = 0;
+    sh.p1 = sh.p2 = UINT32_MAX;
+    sh.ustar = UINT32_MAX;
+    sh.ndoms = 0;
+    sh.nR = 0;
+  }
+  __syncthreads();
+  refresh_kl(T, sh, test);
+  if (sh.csize > sh.h) {
+    if (t == 0) sh.outcome = 1;
+    __syncthreads();
+    return;
+  }
+  if (sh.l <= sh.csize) eval_mindeg(T, sh, test, t_wit);
+  if (sh.rules & R_RED3) {
+    refresh_kl(T, sh, test);
+    const uint32_t c0 = sh.csize;
+    rule3(T, sh);
+    if (sh.csize > sh.h) {
+      if (t == 0) sh.outcome = 1;
+      __syncthreads();
+      return;
+    }
+    if (sh.csize != c0 && sh.l <= sh.csize) eval_mindeg(T, sh, test, t_wit);
+  }
+  if (sh.csize >= sh.h) {
+    if (t == 0) sh.outcome = 1;
+    __syncthreads();
+    return;
+  }
+  rule12(T, sh, test);
+  bounds(T, sh);
+  refresh_kl(T, sh, test);
+  uint32_t ub = min(sh.p1, sh.p2);
+  if (ub <= sh.kl) {
+    if (t == 0) sh.outcome = 2;
+    __syncthreads();
+    return;
+  }
+  if (sh.csize + sh.nR < sh.l) {
+    if (t == 0) sh.outcome = 3;
+    __syncthreads();
+    return;
+  }
+  choose_ustar(T, sh);
+  if (sh.ustar == UINT32_MAX) {
+    if (t == 0) sh.outcome = 3;
+    __syncthreads();
+    return;
+  }
+  find_doms(T, sh);
+  mark_children(T, sh);
+}
+
+__device__ Task make_task(const SearchParams &P, Sh &sh, uint32_t *dyn,
+                          uint32_t cta) {
+  Task T;
+  const uint32_t slot = sh.slot;
+  const size_t st = P.scr.stride;
+  T.W = (sh.n_local <= P.nw_smem) ? dyn : P.scr.word + (size_t)cta * st;
+  T.list = P.scr.list + (size_t)cta * st;
+  T.aux = P.scr.aux + (size_t)cta * st;
+  T.tmp = P.scr.tmp + (size_t)cta * 2 * st;
+  T.dsc = P.scr.dsc + (size_t)cta * st;
+  T.off = P.sa.loc_off + (size_t)slot * (P.sa.stride_n + 1);
+  T.adj = P.sa.loc_adj + (size_t)slot * P.sa.cap_adj;
+  T.dist = P.sa.loc_dist + (size_t)slot * P.sa.stride_n;
+  T.gid = P.sa.loc_gid + (size_t)slot * P.sa.stride_n;
+  T.witness = P.sa.witness + (size_t)slot * P.sa.wit_cap;
+  T.slot = P.slots + slot;
+  return T;
+}
+
+__device__ void set_task_header(const SearchParams &P, Sh &sh,
+                                const uint32_t *rec) {
+  if (threadIdx.x == 0) {
+    sh.slot = rec[0];
+    sh.s = rec[1];
+    sh.csize = rec[2];
+    Slot *sl = P.slots + sh.slot;
+    sh.n_local = sl->n_local;
+    sh.l = sl->l;
+    sh.h = sl->h;
+    sh.ldoms = min(sl->limit_doms, (uint32_t)MAX_DOMS);
+    sh.rules = sl->rules;
+    sh.kl = *(volatile uint32_t *)&sl->kl;
+    sh.q_local = sl->q_local;
+    sh.dmax = P.g.dmax;
+  }
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// test entry: one deterministic step per CTA, all children written in
+// canonical order Include, Dom_0..Dom_{k-1}, Exclude (dead ones skipped)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(BT, 1)
+step_test_kernel(SearchParams P) {
+  extern __shared__ uint32_t dyn[];
+  __shared__ Sh sh;
+  const uint32_t ti = blockIdx.x;
+  if (ti >= P.t_ntasks) return;
+  const uint32_t *rec = P.t_rec + P.t_rec_off[ti];
+  set_task_header(P, sh, rec);
+  if (threadIdx.x == 0) sh.kl = P.t_kl[ti];
+  __syncthreads();
+  Task T = make_task(P, sh, dyn, ti);
+  for (uint32_t i = threadIdx.x; i < sh.n_local && T.W == dyn; i += BT) dyn[i] = 0;
+  __syncthreads();
+  load_record(rec, T, sh);
+  uint32_t *wit = P.t_wit + (size_t)ti * P.t_wit_stride;
+  step_core(T, sh, true, wit);
+  uint32_t *hdr = P.t_hdr + 16 * ti;
+  uint32_t *kids = P.t_kids + (size_t)ti * P.t_kids_stride;
+  if (sh.outcome == 0) {
+    const uint32_t k = sh.ndoms;
+    uint64_t w = 0;
+    uint32_t nk = 0;
+    for (uint32_t code = 0; code <= k + 1; code++) {
+      uint32_t s2, c2;
+      child_shape(sh, code, s2, c2);
+      if (!child_alive(sh, s2, c2)) continue;
+      // layout for the test: [s, csize, entries(s), degrees(s)]
+      uint32_t *dst = kids + w;
+      write_child(T, sh, code, dst + 2, dst + 2 + s2, nullptr);
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        dst[0] = s2;
+        dst[1] = c2;
+      }
+      __syncthreads();
+      w += 2 + 2ull * s2;
+      nk++;
+    }
+    if (threadIdx.x == 0) {
+      hdr[9] = nk;
+      hdr[10] = (uint32_t)w;
+    }
+    clear_aux_list(T, sh);
+  }
+  if (threadIdx.x == 0) {
+    hdr[0] = sh.outcome;
+    hdr[1] = sh.kl;
+    hdr[2] = sh.best;
+    hdr[3] = sh.csize;
+    hdr[4] = sh.outcome >= 2 || sh.outcome == 0 ? sh.csize + sh.nR : 0;
+    hdr[5] = sh.p1;
+    hdr[6] = sh.p2;
+    hdr[7] = sh.ustar;
+    hdr[8] = sh.ndoms;
+    hdr[11] = wit[CL_CAP];
+    for (uint32_t j = 0; j < sh.ndoms; j++)
+      P.t_doms[(size_t)ti * P.t_doms_stride + j] = sh.doms[j];
+  }
+  clear_state(T, sh);
+}
+
+// ---------------------------------------------------------------------------
+// search: persistent within a time slice
+// ---------------------------------------------------------------------------
+__device__ void finish_tasks(const SearchParams &P, uint32_t slot, long long delta) {
+  // delta = children pushed - 1 (per finished task); runs on thread 0
+  Slot *sl = P.slots + slot;
+  unsigned long long old = atomicAdd(&sl->pending, (unsigned long long)delta);
+  atomicAdd(&P.ctr->pending, (unsigned long long)delta);
+  if ((long long)old + delta == 0) {
+    sl->t_done = gtimer();
+    __threadfence();
+    atomicExch(&sl->state, SLOT_DONE);
+    atomicAdd(&P.ctr->done_count, 1u);
+  }
+}
+
+// reserve `len` words for a record: own stack, else the shared pool
+__device__ uint32_t *reserve_record(const SearchParams &P, uint32_t cta,
+                                    uint32_t len, unsigned long long &top,
+                                    unsigned long long &bot, bool &to_pool,
+                                    unsigned long long &pool_off) {
+  uint32_t *base = P.stk.base + (size_t)cta * P.stk.words;
+  to_pool = false;
+  if (top + len <= P.stk.words) {
+    uint32_t *d = base + top;
+    top += len;
+    return d;
+  }
+  // spill to the pool
+  unsigned long long off = atomicAdd(P.pool.arena_top, (unsigned long long)len);
+  if (off + len > P.pool.arena_cap) return nullptr;
+  to_pool = true;
+  pool_off = off;
+  atomicAdd(&P.ctr->spills, 1ull);
+  return P.pool.arena + off;
+}
+
+__device__ bool publish_pool(const SearchParams &P, unsigned long long off) {
+  __threadfence();
+  uint32_t tk = atomicAdd(P.pool.tail, 1u);
+  if (tk >= P.pool.desc_cap) {
+    atomicOr(&P.ctr->error, ERR_POOL);
+    return false;
+  }
+  atomicExch(&P.pool.desc[tk], off + 1ull);
+  return true;
+}
+
+// claim one pool record; returns arena offset+1 or 0
+__device__ unsigned long long pool_take(const SearchParams &P) {
+  for (int attempt = 0; attempt < 64; attempt++) {
+    uint32_t h = *(volatile uint32_t *)P.pool.head;
+    uint32_t tl = min(*(volatile uint32_t *)P.pool.tail, P.pool.desc_cap);
+    if (h >= tl) return 0;
+    if (atomicCAS(P.pool.head, h, h + 1) == h) {
+      for (uint32_t spin = 0; spin < (1u << 24); spin++) {
+        unsigned long long d = *(volatile unsigned long long *)&P.pool.desc[h];
+        if (d) return d;
+        __nanosleep(32);
+      }
+      atomicOr(&P.ctr->error, ERR_SPIN);
+      return 0;
+    }
+  }
+  return 0;
+}
+
+__global__ void __launch_bounds__(BT, 1)
+search_kernel(SearchParams P) {
+  extern __shared__ uint32_t dyn[];
+  __shared__ Sh sh;
+  __shared__ unsigned long long s_top, s_bot;
+  __shared__ int s_hungry;
+  __shared__ uint32_t *s_rec;
+  __shared__ unsigned long long s_pool_off;
+  __shared__ int s_pool_rec;
+  __shared__ unsigned long long s_deadline;
+  const uint32_t cta = blockIdx.x;
+  const int t = threadIdx.x;
+  uint32_t *sbase = P.stk.base + (size_t)cta * P.stk.words;
+  for (uint32_t i = t; i < P.nw_smem; i += BT) dyn[i] = 0;
+  if (t == 0) {
+    unsigned long long want = gtimer() + P.slice_ns;
+    unsigned long long d = atomicCAS(&P.ctr->deadline, 0ull, want);
+    s_deadline = d ? d : want;
+    s_top = P.stk.top[cta];
+    s_bot = P.stk.bot[cta];
+    s_hungry = 0;
+    sh.have = 0;
+    sh.stop = 0;
+  }
+  __syncthreads();
+  Task T;
+  unsigned long long local_nodes = 0;
+  for (;;) {
+    // ---------------- obtain a task ----------------
+    if (!sh.have) {
+      if (t == 0) {
+        s_rec = nullptr;
+        s_pool_rec = 0;
+        if (s_top > s_bot) {
+          uint32_t len = sbase[s_top - 1];
+          if (len < 5 || len > s_top - s_bot) {
+            atomicOr(&P.ctr->error, ERR_RECORD);
+            s_top = s_bot;
+          } else {
+            s_rec = sbase + (s_top - len);
+            s_top -= len;
+          }
+        }
+        if (!s_rec) {
+          unsigned long long d = pool_take(P);
+          if (d) {
+            s_rec = P.pool.arena + (d - 1);
+            s_pool_rec = 1;
+            atomicAdd(&P.ctr->steals, 1ull);
+          }
+        }
+        if (s_rec && s_hungry) {
+          atomicSub(&P.ctr->hungry, 1u);
+          s_hungry = 0;
+        }
+        if (!s_rec) {
+          if (!s_hungry) {
+            atomicAdd(&P.ctr->hungry, 1u);
+            s_hungry = 1;
+          }
+          unsigned long long pend = *(volatile unsigned long long *)&P.ctr->pending;
+          if (pend == 0 || gtimer() > s_deadline ||
+              *(volatile uint32_t *)&P.ctr->stop)
+            sh.stop = 1;
+          else
+            __nanosleep(2000);
+        }
+      }
+      __syncthreads();
+      if (sh.stop) break;
+      if (!s_rec) continue;
+      const uint32_t *rec = s_rec;
+      set_task_header(P, sh, rec);
+      Slot *sl = P.slots + sh.slot;
+      if (*(volatile uint32_t *)&sl->abort) {
+        if (t == 0) finish_tasks(P, sh.slot, -1);
+        __syncthreads();
+        continue;
+      }
+      T = make_task(P, sh, dyn, cta);
+      load_record(rec, T, sh);
+      if (t == 0) sh.have = 1;
+      __syncthreads();
+    }
+    // ---------------- one step ----------------
+    step_core(T, sh, false, nullptr);
+    local_nodes++;
+    uint32_t pushed = 0;
+    bool cont = false;
+    if (sh.outcome == 0) {
+      const uint32_t k = sh.ndoms;
+      // push Exclude, Dom_{k-1} .. Dom_0 (so Dom_0 pops first after the dive)
+      for (int code = (int)k + 1; code >= 1; code--) {
+        uint32_t s2, c2;
+        child_shape(sh, (uint32_t)code, s2, c2);
+        if (!child_alive(sh, s2, c2)) continue;
+        uint32_t len = 2 * s2 + 5;
+        if (t == 0) {
+          bool tp;
+          unsigned long long poff = 0;
+          unsigned long long top = s_top, bot = s_bot;
+          if (top == bot) { top = bot = 0; }
+          uint32_t *d = reserve_record(P, cta, len, top, bot, tp, poff);
+          s_top = top;
+          s_bot = bot;
+          s_rec = d;
+          s_pool_rec = tp ? 1 : 0;
+          s_pool_off = poff;
+          if (!d) {
+            atomicOr(&P.ctr->error, ERR_STACK);
+            P.slots[sh.slot].abort = 1;
+            P.slots[sh.slot].status = RS_CAPACITY;
+          }
+        }
+        __syncthreads();
+        if (!s_rec) continue;
+        {
+          uint32_t *r = s_rec;
+          write_child(T, sh, (uint32_t)code, r + REC_HDR, r + REC_HDR + s2, r);
+        }
+        __syncthreads();
+        if (t == 0 && s_pool_rec) publish_pool(P, s_pool_off);
+        pushed++;
+      }
+      uint32_t s2, c2;
+      child_shape(sh, 0, s2, c2);
+      cont = child_alive(sh, s2, c2);
+      if (cont) {
+        apply_include(T, sh);
+        pushed++;
+      } else {
+        clear_aux_list(T, sh);
+      }
+    }
+    if (t == 0) {
+      finish_tasks(P, sh.slot, (long long)pushed - 1);
+      Slot *sl = P.slots + sh.slot;
+      unsigned long long nd = atomicAdd(&sl->nodes, 1ull) + 1ull;
+      if (sl->node_budget && nd >= sl->node_budget && !sl->abort) {
+        sl->status = RS_TIMEOUT;
+        sl->abort = 1;
+      }
+      sh.have = cont ? 1 : 0;
+    }
+    __syncthreads();
+    if (!cont) clear_state(T, sh);
+    // ---------------- donate the oldest stack record if others are idle ----
+    if (t == 0) {
+      s_rec = nullptr;
+      if (*(volatile uint32_t *)&P.ctr->hungry > 0 && s_top > s_bot) {
+        uint32_t len = sbase[s_bot + 3];
+        if (len >= 5 && s_bot + len < s_top) {  // keep at least one record
+          unsigned long long off = atomicAdd(P.pool.arena_top, (unsigned long long)len);
+          if (off + len <= P.pool.arena_cap) {
+            s_rec = P.pool.arena + off;
+            s_pool_off = off;
+          }
+        }
+      }
+    }
+    __syncthreads();
+    if (s_rec) {
+      const uint32_t *src = sbase + s_bot;
+      const uint32_t len = src[3];
+      for (uint32_t i = t; i < len; i += BT) s_rec[i] = src[i];
+      __syncthreads();
+      if (t == 0) {
+        if (publish_pool(P, s_pool_off)) {
+          s_bot += len;
+          atomicAdd(&P.ctr->donations, 1ull);
+        }
+      }
+      __syncthreads();
+    }
+    // ---------------- leave the slice? ----------------
+    if (t == 0) {
+      if (gtimer() > s_deadline || *(volatile uint32_t *)&P.ctr->stop) sh.stop = 1;
+    }
+    __syncthreads();
+    if (sh.stop) {
+      if (sh.have) {
+        // save the in-place task to the own stack (it is already counted)
+        uint32_t len = 2 * sh.s + 5;
+        if (t == 0) {
+          bool tp;
+          unsigned long long poff = 0;
+          unsigned long long top = s_top, bot = s_bot;
+          if (top == bot) { top = bot = 0; }
+          s_rec = reserve_record(P, cta, len, top, bot, tp, poff);
+          s_top = top;
+          s_bot = bot;
+          s_pool_rec = tp ? 1 : 0;
+          s_pool_off = poff;
+        }
+        __syncthreads();
+        if (s_rec) {
+          uint32_t *d = s_rec;
+          for (uint32_t i = t; i < sh.s; i += BT) {
+            uint32_t x = T.list[i];
+            uint32_t w = T.W[x];
+            d[REC_HDR + i] = (x << 1) | (st_of(w) == ST_C ? 1u : 0u);
+            d[REC_HDR + sh.s + i] = (dc_of(w) << 16) | dr_of(w);
+          }
+          if (t == 0) {
+            d[0] = sh.slot;
+            d[1] = sh.s;
+            d[2] = sh.csize;
+            d[3] = len;
+            d[REC_HDR + 2 * sh.s] = len;
+          }
+          __syncthreads();
+          if (t == 0 && s_pool_rec) publish_pool(P, s_pool_off);
+        } else if (t == 0) {
+          atomicOr(&P.ctr->error, ERR_STACK);
+          P.slots[sh.slot].abort = 1;
+          P.slots[sh.slot].status = RS_CAPACITY;
+          finish_tasks(P, sh.slot, -1);
+        }
+        clear_state(T, sh);
+      }
+      break;
+    }
+  }
+  if (t == 0) {
+    if (s_hungry) atomicSub(&P.ctr->hungry, 1u);
+    if (s_top == s_bot) s_top = s_bot = 0;
+    P.stk.top[cta] = s_top;
+    P.stk.bot[cta] = s_bot;
+    atomicAdd(&P.ctr->nodes, local_nodes);
+  }
+}
+
+size_t search_static_smem() { return sizeof(Sh) + 64; }
+
+}  // namespace scs

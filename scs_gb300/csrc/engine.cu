@@ -1,0 +1,789 @@
+// engine.cu -- the GB300 SCS engine behind include/scs.h.
+//
+// Host flow per query (the reference's processMessages, main.cu:80-473):
+//   submit -> admission into a free slot: ku = min(core[q], h-1)
+//   (inc/Intialize.h:207), greedy incumbent on host threads
+//   (inc/heuristic.h:321-349), early answer when kl == ku (main.cu:122-133),
+//   ubD (main.cu:154-172) -> preprocessing kernel (prep.cu) -> the root task
+//   enters the shared pool -> time-sliced persistent search (bnb.cu) until
+//   the query's outstanding-task count reaches zero -> result.
+// Unlike the reference, admission happens between search slices while other
+// queries keep their tasks on the device (continuous batching), the level
+// loop with its ~15 small copies per level is replaced by one persistent
+// launch per slice, and the engine returns the community itself.
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <deque>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/scs.h"
+#include "host_graph.h"
+#include "scs_device.cuh"
+
+using namespace scs;
+
+namespace {
+
+uint64_t now_ns() {
+  return (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(
+             std::chrono::steady_clock::now().time_since_epoch())
+      .count();
+}
+
+struct Pending {
+  scs_query q;
+  uint64_t ticket;
+  uint64_t t_submit;
+};
+
+struct SlotHost {
+  bool busy = false;
+  Pending p;
+  uint32_t kl_heu = 0;
+  std::vector<uint32_t> heuH;
+};
+
+struct Done {
+  scs_result r;
+  std::vector<uint32_t> H;
+};
+
+std::string g_create_error;
+
+}  // namespace
+
+struct scs_engine {
+  scs_config cfg{};
+  HostGraph g;
+  std::string err;
+  int dev = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+
+  // device graph
+  uint32_t *d_off = nullptr, *d_adj = nullptr, *d_core = nullptr;
+  // slots
+  uint32_t nslots = 0;
+  Slot *d_slots = nullptr;
+  std::vector<Slot> h_slots;
+  SlotArrays sa{};
+  std::vector<SlotHost> slots;
+  // prep
+  uint32_t prep_cap = 0;
+  PrepScratch ps{};
+  PrepJob *d_jobs = nullptr;
+  // search
+  uint32_t grid = 0;
+  uint32_t nw_smem = 0;
+  size_t smem_bytes = 0;
+  Pool pool{};
+  Stacks stk{};
+  Scratch scr{};
+  Counters *d_ctr = nullptr;
+  uint32_t rules = 31;
+  // host state
+  std::deque<Pending> queue;
+  std::deque<Done> done;
+  uint64_t next_ticket = 1;
+  uint32_t running = 0;
+  uint64_t stats[SCS_STAT_COUNT] = {0};
+  std::vector<HeuWork> work;
+  unsigned host_threads = 1;
+  std::vector<void *> allocs;
+
+  int cuda_fail(cudaError_t e, const char *what) {
+    err = std::string(what) + ": " + cudaGetErrorString(e);
+    return SCS_ECUDA;
+  }
+  template <class T>
+  int dalloc(T **p, size_t count, bool zero = true) {
+    size_t bytes = std::max<size_t>(count * sizeof(T), 16);
+    cudaError_t e = cudaMalloc((void **)p, bytes);
+    if (e != cudaSuccess) {
+      err = "cudaMalloc(" + std::to_string(bytes) + "): " + cudaGetErrorString(e);
+      return SCS_ENOMEM;
+    }
+    allocs.push_back(*p);
+    if (zero) {
+      e = cudaMemsetAsync(*p, 0, bytes, stream);
+      if (e != cudaSuccess) return cuda_fail(e, "cudaMemset");
+    }
+    return 0;
+  }
+};
+
+#define CK(call)                                         \
+  do {                                                   \
+    cudaError_t e_ = (call);                             \
+    if (e_ != cudaSuccess) return E->cuda_fail(e_, #call); \
+  } while (0)
+#define RC(call)            \
+  do {                      \
+    int r_ = (call);        \
+    if (r_) return r_;      \
+  } while (0)
+
+static int engine_init(scs_engine *E) {
+  const scs_config &c = E->cfg;
+  E->dev = c.device;
+  CK(cudaSetDevice(E->dev));
+  CK(cudaDeviceGetAttribute(&E->num_sms, cudaDevAttrMultiProcessorCount, E->dev));
+  CK(cudaStreamCreateWithFlags(&E->stream, cudaStreamNonBlocking));
+  CK(cudaEventCreate(&E->ev0));
+  CK(cudaEventCreate(&E->ev1));
+  E->rules = c.rules_set ? ((c.red1 ? R_RED1 : 0) | (c.red2 ? R_RED2 : 0) |
+                            (c.red3 ? R_RED3 : 0) | (c.prun1 ? R_PRUN1 : 0) |
+                            (c.prun2 ? R_PRUN2 : 0))
+                         : 31u;
+  const HostGraph &g = E->g;
+  const uint32_t n = g.n;
+  const uint64_t nnz = g.adj.size();
+  // graph
+  RC(E->dalloc(&E->d_off, n + 1, false));
+  RC(E->dalloc(&E->d_adj, nnz, false));
+  RC(E->dalloc(&E->d_core, n, false));
+  CK(cudaMemcpyAsync(E->d_off, g.off.data(), (n + 1) * 4ull, cudaMemcpyHostToDevice, E->stream));
+  if (nnz) CK(cudaMemcpyAsync(E->d_adj, g.adj.data(), nnz * 4ull, cudaMemcpyHostToDevice, E->stream));
+  CK(cudaMemcpyAsync(E->d_core, g.core.data(), n * 4ull, cudaMemcpyHostToDevice, E->stream));
+  // slots
+  E->nslots = c.limit_queries ? c.limit_queries : 64;
+  E->slots.resize(E->nslots);
+  E->h_slots.resize(E->nslots);
+  RC(E->dalloc(&E->d_slots, E->nslots));
+  SlotArrays &sa = E->sa;
+  sa.stride_n = n;
+  sa.cap_adj = nnz + 3ull * n + 4;
+  sa.wit_cap = CL_CAP;
+  RC(E->dalloc(&sa.loc_off, (size_t)E->nslots * (n + 1), false));
+  RC(E->dalloc(&sa.loc_adj, (size_t)E->nslots * sa.cap_adj, false));
+  RC(E->dalloc(&sa.loc_dist, (size_t)E->nslots * n, false));
+  RC(E->dalloc(&sa.loc_gid, (size_t)E->nslots * n, false));
+  RC(E->dalloc(&sa.witness, (size_t)E->nslots * sa.wit_cap, false));
+  // prep scratch
+  E->prep_cap = std::min<uint32_t>(E->nslots, 256);
+  PrepScratch &ps = E->ps;
+  ps.stride_n = n;
+  ps.stride_w = (n + 31) / 32 + 1;
+  RC(E->dalloc(&ps.dist, (size_t)E->prep_cap * n, false));
+  RC(E->dalloc(&ps.vis, (size_t)E->prep_cap * ps.stride_w, false));
+  RC(E->dalloc(&ps.comp, (size_t)E->prep_cap * ps.stride_w, false));
+  RC(E->dalloc(&ps.fa, (size_t)E->prep_cap * n, false));
+  RC(E->dalloc(&ps.fb, (size_t)E->prep_cap * n, false));
+  RC(E->dalloc(&ps.wpre, (size_t)E->prep_cap * ps.stride_w, false));
+  RC(E->dalloc(&E->d_jobs, E->prep_cap));
+  // search grid and shared memory
+  int max_optin = 0;
+  CK(cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, E->dev));
+  uint32_t cps = c.ctas_per_sm ? c.ctas_per_sm : 1;
+  size_t stat = search_static_smem();
+  size_t budget = (size_t)max_optin;
+  if (cps > 1) budget = std::min(budget, (size_t)(228 * 1024) / cps - 1024);
+  size_t words = budget > stat ? (budget - stat) / 4 : 0;
+  E->nw_smem = (uint32_t)std::min<size_t>(words, std::min<uint32_t>(n, MAX_LOCAL));
+  E->smem_bytes = (size_t)E->nw_smem * 4;
+  CK(cudaFuncSetAttribute(search_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                          (int)E->smem_bytes));
+  CK(cudaFuncSetAttribute(step_test_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                          (int)E->smem_bytes));
+  int occ = 0;
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, search_kernel, SEARCH_THREADS,
+                                                   E->smem_bytes));
+  if (occ < 1) {
+    E->err = "search kernel does not fit on an SM";
+    return SCS_ECUDA;
+  }
+  cps = std::min<uint32_t>(cps, (uint32_t)occ);
+  E->grid = (uint32_t)E->num_sms * cps;
+  // per-CTA scratch
+  Scratch &sc = E->scr;
+  sc.stride = n + 4;
+  RC(E->dalloc(&sc.word, (size_t)E->grid * sc.stride));
+  RC(E->dalloc(&sc.list, (size_t)E->grid * sc.stride, false));
+  RC(E->dalloc(&sc.aux, (size_t)E->grid * sc.stride));
+  RC(E->dalloc(&sc.tmp, (size_t)E->grid * 2 * sc.stride, false));
+  RC(E->dalloc(&sc.dsc, (size_t)E->grid * sc.stride, false));
+  // stacks
+  size_t free_b = 0, total_b = 0;
+  CK(cudaMemGetInfo(&free_b, &total_b));
+  uint64_t sw = c.stack_words;
+  if (!sw) {
+    // a few hundred root-sized records per CTA, capped by 40% of free memory
+    uint64_t want = std::max<uint64_t>(1ull << 20, (uint64_t)(2 * n + 5) * 256);
+    uint64_t cap = (uint64_t)(free_b * 0.4) / 4 / E->grid;
+    sw = std::min(want, cap);
+  }
+  E->stk.words = sw;
+  RC(E->dalloc(&E->stk.base, (size_t)E->grid * sw, false));
+  RC(E->dalloc(&E->stk.top, E->grid));
+  RC(E->dalloc(&E->stk.bot, E->grid));
+  // pool
+  CK(cudaMemGetInfo(&free_b, &total_b));
+  uint64_t pw = c.pool_words;
+  if (!pw) pw = std::min<uint64_t>((uint64_t)(free_b * 0.5) / 4, 1ull << 31);
+  E->pool.arena_cap = pw;
+  RC(E->dalloc(&E->pool.arena, pw, false));
+  RC(E->dalloc(&E->pool.arena_top, 1));
+  E->pool.desc_cap = 1u << 22;
+  RC(E->dalloc(&E->pool.desc, E->pool.desc_cap));
+  RC(E->dalloc(&E->pool.head, 1));
+  RC(E->dalloc(&E->pool.tail, 1));
+  RC(E->dalloc(&E->d_ctr, 1));
+  CK(cudaStreamSynchronize(E->stream));
+  E->host_threads = c.host_threads ? c.host_threads
+                                   : std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  E->work.resize(E->host_threads);
+  return 0;
+}
+
+static SearchParams make_params(scs_engine *E) {
+  SearchParams P{};
+  P.g = DevGraph{E->g.n, E->g.dmax, E->d_off, E->d_adj, E->d_core};
+  P.sa = E->sa;
+  P.slots = E->d_slots;
+  P.pool = E->pool;
+  P.ctr = E->d_ctr;
+  P.stk = E->stk;
+  P.scr = E->scr;
+  P.nw_smem = E->nw_smem;
+  return P;
+}
+
+static void finish_result(scs_engine *E, uint32_t si, uint32_t degree,
+                          int32_t status, uint64_t nodes, uint64_t search_ns,
+                          const std::vector<uint32_t> &H) {
+  SlotHost &sh = E->slots[si];
+  Done d;
+  d.r.ticket = sh.p.ticket;
+  d.r.l = sh.p.q.l;
+  d.r.h = sh.p.q.h;
+  d.r.q = sh.p.q.q;
+  d.r.degree = degree;
+  d.r.status = status;
+  d.r.kl_heuristic = sh.kl_heu;
+  d.r.nodes = nodes;
+  d.r.search_ns = search_ns;
+  d.H = H;
+  d.r.h_size = (uint32_t)H.size();
+  uint32_t md = 0;
+  bool ok = verify_community(E->g, H.data(), (uint32_t)H.size(), sh.p.q.q,
+                             sh.p.q.l, sh.p.q.h, md);
+  d.r.h_verified = (ok && md == degree) ? 1u : 0u;
+  d.r.latency_ns = now_ns() - sh.p.t_submit;
+  E->done.push_back(std::move(d));
+  sh.busy = false;
+}
+
+// Finish queries answered without a search (bad input, heuristic hit).
+static void finish_now(scs_engine *E, const Pending &p, uint32_t degree,
+                       int32_t status, uint32_t kl_heu,
+                       const std::vector<uint32_t> &H) {
+  Done d;
+  d.r.ticket = p.ticket;
+  d.r.l = p.q.l;
+  d.r.h = p.q.h;
+  d.r.q = p.q.q;
+  d.r.degree = degree;
+  d.r.status = status;
+  d.r.kl_heuristic = kl_heu;
+  d.H = H;
+  d.r.h_size = (uint32_t)H.size();
+  uint32_t md = 0;
+  bool ok = status != SCS_BAD_QUERY &&
+            verify_community(E->g, H.data(), (uint32_t)H.size(), p.q.q, p.q.l,
+                             p.q.h, md);
+  d.r.h_verified = (ok && md == degree) ? 1u : 0u;
+  d.r.latency_ns = now_ns() - p.t_submit;
+  E->done.push_back(std::move(d));
+}
+
+// Admit queued queries into free slots; returns the number of prep jobs.
+static int admit(scs_engine *E) {
+  std::vector<uint32_t> free_slots;
+  for (uint32_t i = 0; i < E->nslots; i++)
+    if (!E->slots[i].busy) free_slots.push_back(i);
+  std::vector<Pending> batch;
+  while (!E->queue.empty() && batch.size() < free_slots.size() &&
+         batch.size() < E->prep_cap) {
+    batch.push_back(E->queue.front());
+    E->queue.pop_front();
+  }
+  if (batch.empty()) return 0;
+  const uint32_t n = E->g.n;
+  struct Adm {
+    bool bad = false;
+    uint32_t kl = 0, ku = 0;
+    std::vector<uint32_t> H;
+  };
+  std::vector<Adm> adm(batch.size());
+  // greedy incumbents on host threads
+  {
+    std::atomic<size_t> next{0};
+    auto worker = [&](unsigned tid) {
+      for (;;) {
+        size_t i = next.fetch_add(1);
+        if (i >= batch.size()) break;
+        const scs_query &q = batch[i].q;
+        Adm &a = adm[i];
+        if (q.q >= n || q.h < 1 || q.h >= CL_CAP - 1 || q.l > q.h) {
+          a.bad = true;
+          continue;
+        }
+        a.ku = std::min(E->g.core[q.q], q.h - 1);
+        if (q.heuristic) a.kl = greedy_incumbent(E->g, q.l, q.h, q.q, E->work[tid], a.H);
+      }
+    };
+    unsigned nt = std::min<unsigned>(E->host_threads, (unsigned)batch.size());
+    std::vector<std::thread> th;
+    for (unsigned k = 1; k < nt; k++) th.emplace_back(worker, k);
+    worker(0);
+    for (auto &t : th) t.join();
+  }
+  std::vector<PrepJob> jobs;
+  size_t fs = 0;
+  for (size_t i = 0; i < batch.size(); i++) {
+    const Pending &p = batch[i];
+    Adm &a = adm[i];
+    if (a.bad) {
+      finish_now(E, p, 0, SCS_BAD_QUERY, 0, {});
+      continue;
+    }
+    if (a.kl == a.ku || E->g.core[p.q.q] <= a.kl) {
+      // the incumbent is optimal (main.cu:122-133), or no community better
+      // than kl can contain q (core[q] <= kl)
+      finish_now(E, p, a.kl, a.kl == a.ku ? SCS_HEURISTIC : SCS_DONE, a.kl, a.H);
+      continue;
+    }
+    uint32_t si = free_slots[fs++];
+    SlotHost &sh = E->slots[si];
+    sh.busy = true;
+    sh.p = p;
+    sh.kl_heu = a.kl;
+    sh.heuH = a.H;
+    PrepJob j{};
+    j.slot = si;
+    j.q = p.q.q;
+    j.kl = a.kl;
+    j.ubd = ubd_host(a.kl, p.q.h);
+    j.l = p.q.l;
+    j.h = p.q.h;
+    j.limit_doms = std::min<uint32_t>(p.q.limit_doms, MAX_DOMS);
+    j.rules = E->rules;
+    j.kl_heu = a.kl;
+    j.root_to_pool = 1;
+    j.node_budget = E->cfg.node_budget;
+    jobs.push_back(j);
+  }
+  if (jobs.empty()) return 0;
+  cudaMemcpyAsync(E->d_jobs, jobs.data(), jobs.size() * sizeof(PrepJob),
+                  cudaMemcpyHostToDevice, E->stream);
+  prep_kernel<<<(unsigned)jobs.size(), PREP_THREADS, 0, E->stream>>>(
+      DevGraph{n, E->g.dmax, E->d_off, E->d_adj, E->d_core}, E->sa, E->d_slots,
+      E->d_jobs, (int)jobs.size(), E->ps, E->pool, E->d_ctr);
+  E->stats[SCS_STAT_LAUNCHES]++;
+  E->running += (uint32_t)jobs.size();
+  return (int)jobs.size();
+}
+
+// one search slice + collection of finished slots
+static int slice(scs_engine *E) {
+  uint64_t t_us = E->cfg.slice_us ? E->cfg.slice_us : 20000;
+  SearchParams P = make_params(E);
+  P.slice_ns = t_us * 1000ull;
+  // per-slice fields: deadline (set by the first CTA), hungry, error,
+  // done_count, stop
+  CK(cudaMemsetAsync(&E->d_ctr->deadline, 0, 8, E->stream));
+  CK(cudaMemsetAsync(&E->d_ctr->hungry, 0, sizeof(uint32_t) * 4, E->stream));
+  CK(cudaEventRecord(E->ev0, E->stream));
+  search_kernel<<<E->grid, SEARCH_THREADS, E->smem_bytes, E->stream>>>(P);
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(E->ev1, E->stream));
+  E->stats[SCS_STAT_LAUNCHES]++;
+  E->stats[SCS_STAT_SLICES]++;
+  // read back slots and counters
+  CK(cudaMemcpyAsync(E->h_slots.data(), E->d_slots, E->nslots * sizeof(Slot),
+                     cudaMemcpyDeviceToHost, E->stream));
+  Counters hc;
+  CK(cudaMemcpyAsync(&hc, E->d_ctr, sizeof(Counters), cudaMemcpyDeviceToHost, E->stream));
+  uint32_t ph[2];
+  CK(cudaMemcpyAsync(ph, E->pool.head, 4, cudaMemcpyDeviceToHost, E->stream));
+  CK(cudaMemcpyAsync(ph + 1, E->pool.tail, 4, cudaMemcpyDeviceToHost, E->stream));
+  CK(cudaStreamSynchronize(E->stream));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, E->ev0, E->ev1);
+  E->stats[SCS_STAT_SEARCH_NS] += (uint64_t)(ms * 1e6);
+  E->stats[SCS_STAT_NODES] = hc.nodes;
+  E->stats[SCS_STAT_DONATIONS] = hc.donations;
+  E->stats[SCS_STAT_STEALS] = hc.steals;
+  E->stats[SCS_STAT_SPILLS] = hc.spills;
+  E->stats[SCS_STAT_PREP_BYTES] = hc.prep_bytes;
+  if (hc.error) {
+    E->err = "device error flags " + std::to_string(hc.error);
+    E->stats[SCS_STAT_COUNT - 1] |= hc.error;
+  }
+  // collect finished slots
+  for (uint32_t i = 0; i < E->nslots; i++) {
+    SlotHost &sh = E->slots[i];
+    const Slot &s = E->h_slots[i];
+    if (!sh.busy || s.state != SLOT_DONE) continue;
+    uint32_t degree = s.kl;
+    std::vector<uint32_t> H;
+    uint32_t wv = s.wit_val ? s.wit_val - 1 : 0;
+    if (s.wit_val && wv == degree && s.wit_n) {
+      H.resize(s.wit_n);
+      CK(cudaMemcpy(H.data(), E->sa.witness + (size_t)i * E->sa.wit_cap,
+                    s.wit_n * 4ull, cudaMemcpyDeviceToHost));
+    } else {
+      H = sh.heuH;
+    }
+    int32_t st = (int32_t)s.status;
+    uint64_t sns = s.t_done > s.t_admit ? s.t_done - s.t_admit : 0;
+    finish_result(E, i, degree, st, s.nodes, sns, H);
+    Slot clear{};
+    CK(cudaMemcpyAsync(E->d_slots + i, &clear, sizeof(Slot), cudaMemcpyHostToDevice, E->stream));
+    E->running--;
+  }
+  // pool reset when fully drained
+  if (ph[0] >= std::min(ph[1], E->pool.desc_cap) && ph[1] > 0) {
+    uint32_t used = std::min(ph[1], E->pool.desc_cap);
+    CK(cudaMemsetAsync(E->pool.desc, 0, used * 8ull, E->stream));
+    CK(cudaMemsetAsync(E->pool.arena_top, 0, 8, E->stream));
+    CK(cudaMemsetAsync(E->pool.head, 0, 4, E->stream));
+    CK(cudaMemsetAsync(E->pool.tail, 0, 4, E->stream));
+  }
+  CK(cudaStreamSynchronize(E->stream));
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+static int create_common(scs_engine **out, scs_engine *E, const scs_config *cfg) {
+  if (cfg) E->cfg = *cfg;
+  int rc = engine_init(E);
+  if (rc) {
+    g_create_error = E->err;
+    scs_destroy(E);
+    *out = nullptr;
+    return rc;
+  }
+  *out = E;
+  return 0;
+}
+
+int scs_create(scs_engine **out, const char *path, const scs_config *cfg) {
+  if (!out || !path) return SCS_EINVAL;
+  scs_engine *E = new scs_engine();
+  int rc = load_edge_list(path, E->g, E->err);
+  if (rc) {
+    g_create_error = E->err;
+    delete E;
+    *out = nullptr;
+    return SCS_EIO;
+  }
+  return create_common(out, E, cfg);
+}
+
+int scs_create_csr(scs_engine **out, uint32_t n, const uint32_t *off,
+                   const uint32_t *adj, const scs_config *cfg) {
+  if (!out) return SCS_EINVAL;
+  scs_engine *E = new scs_engine();
+  if (adopt_csr(n, off, adj, E->g, E->err)) {
+    g_create_error = E->err;
+    delete E;
+    *out = nullptr;
+    return SCS_EINVAL;
+  }
+  return create_common(out, E, cfg);
+}
+
+int scs_graph_info(scs_engine *E, uint32_t *n, uint64_t *nnz, uint32_t *dmax) {
+  if (!E) return SCS_EINVAL;
+  if (n) *n = E->g.n;
+  if (nnz) *nnz = E->g.adj.size();
+  if (dmax) *dmax = E->g.dmax;
+  return 0;
+}
+
+int scs_core_numbers(scs_engine *E, uint32_t *core) {
+  if (!E || !core) return SCS_EINVAL;
+  std::copy(E->g.core.begin(), E->g.core.end(), core);
+  return 0;
+}
+
+int scs_submit(scs_engine *E, const scs_query *q, uint64_t *ticket) {
+  if (!E || !q) return SCS_EINVAL;
+  Pending p;
+  p.q = *q;
+  p.ticket = E->next_ticket++;
+  p.t_submit = now_ns();
+  E->queue.push_back(p);
+  if (ticket) *ticket = p.ticket;
+  return 0;
+}
+
+int scs_step(scs_engine *E) {
+  if (!E) return SCS_EINVAL;
+  int a = admit(E);
+  if (a < 0) return a;
+  if (E->running > 0) RC(slice(E));
+  return (int)(E->queue.size() + E->running);
+}
+
+int scs_run(scs_engine *E) {
+  if (!E) return SCS_EINVAL;
+  for (;;) {
+    int r = scs_step(E);
+    if (r < 0) return r;
+    if (r == 0) return 0;
+  }
+}
+
+int scs_poll(scs_engine *E, scs_result *out, int max, uint32_t *h_buf,
+             uint32_t h_stride) {
+  if (!E || (!out && max > 0)) return SCS_EINVAL;
+  int k = 0;
+  while (k < max && !E->done.empty()) {
+    Done &d = E->done.front();
+    out[k] = d.r;
+    if (h_buf) {
+      uint32_t c = std::min<uint32_t>(d.r.h_size, h_stride);
+      std::copy(d.H.begin(), d.H.begin() + c, h_buf + (size_t)k * h_stride);
+    }
+    E->done.pop_front();
+    k++;
+  }
+  return k;
+}
+
+int scs_stats(scs_engine *E, uint64_t *out) {
+  if (!E || !out) return SCS_EINVAL;
+  std::copy(E->stats, E->stats + SCS_STAT_COUNT, out);
+  return 0;
+}
+
+const char *scs_last_error(scs_engine *E) {
+  return E ? E->err.c_str() : g_create_error.c_str();
+}
+
+int scs_destroy(scs_engine *E) {
+  if (!E) return SCS_EINVAL;
+  if (E->stream) cudaStreamSynchronize(E->stream);
+  for (void *p : E->allocs) cudaFree(p);
+  if (E->ev0) cudaEventDestroy(E->ev0);
+  if (E->ev1) cudaEventDestroy(E->ev1);
+  if (E->stream) cudaStreamDestroy(E->stream);
+  delete E;
+  return 0;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// test hooks
+// ---------------------------------------------------------------------------
+extern "C" {
+
+int scs_debug_prepare(scs_engine *E, uint32_t nq, const scs_query *qs,
+                      const uint32_t *kl, const uint32_t *ubd,
+                      uint32_t *n_local, uint32_t *q_local) {
+  if (!E || !qs || !kl || !ubd) return SCS_EINVAL;
+  if (nq > E->nslots || nq > E->prep_cap || E->running) return SCS_EBUSY;
+  std::vector<PrepJob> jobs(nq);
+  for (uint32_t i = 0; i < nq; i++) {
+    if (qs[i].q >= E->g.n || qs[i].h < 1 || qs[i].h >= CL_CAP - 1) return SCS_EINVAL;
+    PrepJob &j = jobs[i];
+    j = PrepJob{};
+    j.slot = i;
+    j.q = qs[i].q;
+    j.kl = kl[i];
+    j.ubd = ubd[i];
+    j.l = qs[i].l;
+    j.h = qs[i].h;
+    j.limit_doms = std::min<uint32_t>(qs[i].limit_doms, MAX_DOMS);
+    j.rules = E->rules;
+    j.kl_heu = kl[i];
+    j.root_to_pool = 0;
+  }
+  CK(cudaMemcpyAsync(E->d_jobs, jobs.data(), nq * sizeof(PrepJob),
+                     cudaMemcpyHostToDevice, E->stream));
+  prep_kernel<<<nq, PREP_THREADS, 0, E->stream>>>(
+      DevGraph{E->g.n, E->g.dmax, E->d_off, E->d_adj, E->d_core}, E->sa,
+      E->d_slots, E->d_jobs, (int)nq, E->ps, E->pool, E->d_ctr);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(E->h_slots.data(), E->d_slots, nq * sizeof(Slot),
+                     cudaMemcpyDeviceToHost, E->stream));
+  CK(cudaStreamSynchronize(E->stream));
+  for (uint32_t i = 0; i < nq; i++) {
+    if (n_local) n_local[i] = E->h_slots[i].n_local;
+    if (q_local) q_local[i] = E->h_slots[i].q_local;
+    if (E->h_slots[i].status == RS_TOO_LARGE) return SCS_EINVAL;
+  }
+  return 0;
+}
+
+// Local graph of a prepared slot with padding removed.
+int scs_debug_local_graph(scs_engine *E, uint32_t slot, uint32_t *gid,
+                          uint32_t *off, uint32_t *adj, uint32_t *dist) {
+  if (!E || slot >= E->nslots) return SCS_EINVAL;
+  CK(cudaMemcpy(&E->h_slots[slot], E->d_slots + slot, sizeof(Slot), cudaMemcpyDeviceToHost));
+  const uint32_t nl = E->h_slots[slot].n_local;
+  const uint32_t n = E->g.n;
+  std::vector<uint32_t> loff(nl + 1);
+  CK(cudaMemcpy(loff.data(), E->sa.loc_off + (size_t)slot * (n + 1), (nl + 1) * 4ull,
+                cudaMemcpyDeviceToHost));
+  std::vector<uint32_t> ladj(loff[nl]);
+  if (loff[nl])
+    CK(cudaMemcpy(ladj.data(), E->sa.loc_adj + (size_t)slot * E->sa.cap_adj,
+                  loff[nl] * 4ull, cudaMemcpyDeviceToHost));
+  if (gid)
+    CK(cudaMemcpy(gid, E->sa.loc_gid + (size_t)slot * n, nl * 4ull, cudaMemcpyDeviceToHost));
+  if (dist) {
+    std::vector<uint16_t> d16(nl);
+    CK(cudaMemcpy(d16.data(), E->sa.loc_dist + (size_t)slot * n, nl * 2ull,
+                  cudaMemcpyDeviceToHost));
+    for (uint32_t i = 0; i < nl; i++) dist[i] = d16[i] == INF16 ? 1000000000u : d16[i];
+  }
+  uint64_t w = 0;
+  if (off) off[0] = 0;
+  for (uint32_t i = 0; i < nl; i++) {
+    for (uint32_t k = loff[i]; k < loff[i + 1]; k++)
+      if (ladj[k] != SENT) {
+        if (adj) adj[w] = ladj[k];
+        w++;
+      }
+    if (off) off[i + 1] = (uint32_t)w;
+  }
+  return 0;
+}
+
+// One deterministic step per task on prepared slots.  Task entries are
+// (local_id<<1)|inC, ascending; the input degrees are computed here from the
+// slot's local graph.
+int scs_debug_step(scs_engine *E, uint32_t ntasks, const uint32_t *task_slot,
+                   const uint32_t *kl_in, const uint64_t *task_off,
+                   const uint32_t *task_len, const uint32_t *task_entries,
+                   uint32_t *out_hdr, uint32_t *out_doms, uint32_t doms_stride,
+                   uint32_t *out_kids, uint64_t kids_stride, uint32_t *out_wit,
+                   uint32_t wit_stride) {
+  if (!E || !ntasks) return SCS_EINVAL;
+  if (wit_stride < CL_CAP + 1 || doms_stride < MAX_DOMS) return SCS_EINVAL;
+  const uint32_t n = E->g.n;
+  // local graphs of the slots used
+  std::vector<std::vector<uint32_t>> loff(E->nslots), ladj(E->nslots);
+  for (uint32_t t = 0; t < ntasks; t++) {
+    uint32_t s = task_slot[t];
+    if (s >= E->nslots) return SCS_EINVAL;
+    if (!loff[s].empty()) continue;
+    CK(cudaMemcpy(&E->h_slots[s], E->d_slots + s, sizeof(Slot), cudaMemcpyDeviceToHost));
+    uint32_t nl = E->h_slots[s].n_local;
+    loff[s].resize(nl + 1);
+    std::vector<uint32_t> o(nl + 1), a(n + 1);
+    int rc = scs_debug_local_graph(E, s, nullptr, o.data(), nullptr, nullptr);
+    if (rc) return rc;
+    std::vector<uint32_t> aa(o[nl] + 1);
+    rc = scs_debug_local_graph(E, s, nullptr, o.data(), aa.data(), nullptr);
+    if (rc) return rc;
+    loff[s] = o;
+    ladj[s] = aa;
+  }
+  // records with degrees
+  std::vector<uint32_t> recs;
+  std::vector<unsigned long long> roff(ntasks);
+  std::vector<int32_t> pos(n, -1);
+  for (uint32_t t = 0; t < ntasks; t++) {
+    uint32_t s = task_slot[t], len = task_len[t];
+    const uint32_t *e = task_entries + task_off[t];
+    roff[t] = recs.size();
+    recs.resize(recs.size() + 2 * len + 5);
+    uint32_t *r = recs.data() + roff[t];
+    uint32_t cs = 0;
+    for (uint32_t i = 0; i < len; i++) pos[e[i] >> 1] = (int32_t)i;
+    for (uint32_t i = 0; i < len; i++) {
+      uint32_t v = e[i] >> 1, dc = 0, dr = 0;
+      cs += e[i] & 1u;
+      for (uint32_t k = loff[s][v]; k < loff[s][v + 1]; k++) {
+        int32_t j = pos[ladj[s][k]];
+        if (j >= 0) {
+          if (e[j] & 1u) dc++;
+          else dr++;
+        }
+      }
+      r[REC_HDR + i] = e[i];
+      r[REC_HDR + len + i] = (dc << 16) | dr;
+    }
+    for (uint32_t i = 0; i < len; i++) pos[e[i] >> 1] = -1;
+    r[0] = s;
+    r[1] = len;
+    r[2] = cs;
+    r[3] = 2 * len + 5;
+    r[REC_HDR + 2 * len] = 2 * len + 5;
+  }
+  uint32_t *d_rec = nullptr, *d_hdr = nullptr, *d_doms = nullptr, *d_kids = nullptr,
+           *d_wit = nullptr, *d_kl = nullptr;
+  unsigned long long *d_roff = nullptr;
+  int rc = 0;
+  auto cleanup = [&]() {
+    cudaFree(d_rec); cudaFree(d_hdr); cudaFree(d_doms); cudaFree(d_kids);
+    cudaFree(d_wit); cudaFree(d_kl); cudaFree(d_roff);
+  };
+  const uint32_t chunk = E->grid;
+  for (uint32_t base = 0; base < ntasks && !rc; base += chunk) {
+    uint32_t cnt = std::min(chunk, ntasks - base);
+    if (!d_rec) {
+      if (cudaMalloc(&d_rec, recs.size() * 4) || cudaMalloc(&d_roff, ntasks * 8ull) ||
+          cudaMalloc(&d_hdr, 16ull * chunk * 4) ||
+          cudaMalloc(&d_doms, (size_t)doms_stride * chunk * 4) ||
+          cudaMalloc(&d_kids, kids_stride * chunk * 4) ||
+          cudaMalloc(&d_wit, (size_t)wit_stride * chunk * 4) ||
+          cudaMalloc(&d_kl, ntasks * 4ull)) {
+        cleanup();
+        E->err = "debug step allocation failed";
+        return SCS_ENOMEM;
+      }
+      cudaMemcpy(d_rec, recs.data(), recs.size() * 4, cudaMemcpyHostToDevice);
+      cudaMemcpy(d_roff, roff.data(), ntasks * 8ull, cudaMemcpyHostToDevice);
+      cudaMemcpy(d_kl, kl_in, ntasks * 4ull, cudaMemcpyHostToDevice);
+    }
+    cudaMemset(d_hdr, 0, 16ull * chunk * 4);
+    cudaMemset(d_wit, 0, (size_t)wit_stride * chunk * 4);
+    SearchParams P = make_params(E);
+    P.t_rec = d_rec;
+    P.t_rec_off = d_roff + base;
+    P.t_ntasks = cnt;
+    P.t_hdr = d_hdr;
+    P.t_doms = d_doms;
+    P.t_doms_stride = doms_stride;
+    P.t_kids = d_kids;
+    P.t_kids_stride = kids_stride;
+    P.t_wit = d_wit;
+    P.t_wit_stride = wit_stride;
+    P.t_kl = d_kl + base;
+    step_test_kernel<<<cnt, SEARCH_THREADS, E->smem_bytes, E->stream>>>(P);
+    cudaError_t e = cudaStreamSynchronize(E->stream);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) {
+      cleanup();
+      return E->cuda_fail(e, "step_test_kernel");
+    }
+    cudaMemcpy(out_hdr + 16ull * base, d_hdr, 16ull * cnt * 4, cudaMemcpyDeviceToHost);
+    cudaMemcpy(out_doms + (size_t)doms_stride * base, d_doms, (size_t)doms_stride * cnt * 4,
+               cudaMemcpyDeviceToHost);
+    cudaMemcpy(out_kids + kids_stride * base, d_kids, kids_stride * cnt * 4,
+               cudaMemcpyDeviceToHost);
+    cudaMemcpy(out_wit + (size_t)wit_stride * base, d_wit, (size_t)wit_stride * cnt * 4,
+               cudaMemcpyDeviceToHost);
+  }
+  cleanup();
+  return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,200 @@
+// scs_device.cuh -- device data layout shared by the preprocessing and the
+// branch-and-bound kernels.
+//
+// Layout in HBM (one engine, one GPU):
+//   graph      : CSR off[n+1], adj[nnz] (ascending), core[n]    (resident)
+//   slot i     : local graph of query i -- loc_off[n+1], loc_adj[cap_adj]
+//                (rows padded to a multiple of 4 with SENT so rows can be read
+//                with 16-byte loads), loc_dist[n] (u16), loc_gid[n], witness
+//   CTA c      : task stack region (LIFO, records below), scratch arrays
+//   pool       : shared arena + descriptor ring for tasks moved between CTAs
+//
+// Task record (u32 words):
+//   [0] slot  [1] s  [2] csize  [3] len
+//   [4 .. 4+s)      entries  (local_id << 1) | inC      (ascending id)
+//   [4+s .. 4+2s)   degrees  (dC << 16) | dR            (within the task)
+//   [4+2s]          footer = len = 2s + 5
+// Per-vertex state word used while a CTA works on a task (shared memory):
+//   bits 31..30 status (0 absent, 1 R, 2 C, 3 removed), 29..15 dC, 14..0 dR.
+#pragma once
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+namespace scs {
+
+constexpr uint32_t SENT = 0xFFFFFFFFu;
+constexpr uint32_t ST_ABSENT = 0, ST_R = 1, ST_C = 2, ST_X = 3;
+constexpr uint32_t DC_ONE = 1u << 15;
+constexpr uint32_t ST_ONE = 1u << 30;
+constexpr uint32_t DMASK = 0x7FFFu;
+constexpr uint32_t MAX_LOCAL = 32768;  // 15-bit in-task degree fields
+constexpr uint32_t CL_CAP = 512;       // max |C| tracked (h < CL_CAP)
+constexpr uint32_t MAX_DOMS = 15;      // adjacency mask bits 1..15
+constexpr uint32_t INF16 = 0xFFFFu;
+constexpr uint32_t REC_HDR = 4;
+
+// rule switches (same bits as the oracle): red1 red2 red3 prun1 prun2
+constexpr uint32_t R_RED1 = 1, R_RED2 = 2, R_RED3 = 4, R_PRUN1 = 8,
+                   R_PRUN2 = 16;
+
+// slot states
+constexpr uint32_t SLOT_FREE = 0, SLOT_SEARCH = 2, SLOT_DONE = 3;
+
+// result status (mirrors scs.h)
+constexpr uint32_t RS_DONE = 0, RS_HEURISTIC = 1, RS_CAPACITY = 2,
+                   RS_TIMEOUT = 3, RS_BAD = 4, RS_TOO_LARGE = 5;
+
+struct Slot {
+  uint32_t state;
+  uint32_t status;
+  uint32_t n_local;
+  uint32_t q_local;
+  uint32_t l, h, limit_doms, rules;
+  uint32_t kl;       // incumbent, atomicMax
+  uint32_t kl_heu;
+  uint32_t ubd;
+  uint32_t wit_lock;
+  uint32_t wit_val;  // min degree of the witness (0 = none)
+  uint32_t wit_n;
+  uint32_t q_global;
+  uint32_t abort;    // set when the query stops early (budget/capacity)
+  unsigned long long pending;  // outstanding tasks of this query
+  unsigned long long nodes;
+  unsigned long long t_admit;
+  unsigned long long t_done;
+  unsigned long long node_budget;
+};
+
+struct DevGraph {
+  uint32_t n;
+  uint32_t dmax;
+  const uint32_t *off;
+  const uint32_t *adj;
+  const uint32_t *core;
+};
+
+struct SlotArrays {
+  uint32_t *loc_off;  // [slots][n+1]
+  uint32_t *loc_adj;  // [slots][cap_adj]
+  uint16_t *loc_dist; // [slots][n]
+  uint32_t *loc_gid;  // [slots][n]
+  uint32_t *witness;  // [slots][wit_cap]
+  uint64_t cap_adj;
+  uint32_t stride_n;
+  uint32_t wit_cap;
+};
+
+struct Pool {
+  uint32_t *arena;
+  unsigned long long arena_cap;   // words
+  unsigned long long *arena_top;  // bump pointer (words)
+  unsigned long long *desc;       // offset+1, 0 = not yet published
+  uint32_t desc_cap;
+  uint32_t *head;
+  uint32_t *tail;
+};
+
+struct Counters {
+  unsigned long long pending;  // outstanding tasks, all queries
+  unsigned long long nodes;
+  unsigned long long donations;
+  unsigned long long steals;
+  unsigned long long spills;
+  unsigned long long bytes;
+  unsigned long long prep_bytes;
+  unsigned long long deadline; // set by the first CTA of a slice
+  uint32_t hungry;
+  uint32_t error;              // bit flags, see ERR_*
+  uint32_t done_count;
+  uint32_t stop;               // host asks CTAs to leave the slice
+  uint32_t err_info[4];
+};
+
+constexpr uint32_t ERR_SPIN = 1, ERR_POOL = 2, ERR_STACK = 4, ERR_RECORD = 8;
+
+struct Stacks {
+  uint32_t *base;                  // [ctas][words]
+  unsigned long long words;        // per CTA
+  unsigned long long *top;         // [ctas]
+  unsigned long long *bot;         // [ctas]
+};
+
+struct Scratch {  // per search CTA, stride n words each
+  uint32_t *word;  // fallback state words when n_local exceeds shared memory
+  uint32_t *list;  // live ids of the current task (ascending)
+  uint32_t *aux;   // marks (zero between uses)
+  uint32_t *tmp;   // removal / promotion / candidate lists
+  double *dsc;     // candidate scores
+  uint32_t stride;
+};
+
+__host__ __device__ inline uint32_t ubd_dev(uint32_t kl, uint32_t h) {
+  // distance bound of src/helpers.cc:974-990, u32 arithmetic as written
+  uint32_t ubd = h - 1;
+  for (uint32_t d = 1; d <= h; d++) {
+    if (d == 1 || d == 2) {
+      if (kl + d > h) { ubd = d - 1; break; }
+    } else {
+      uint32_t min_n = kl + d + 1 + (d / 3) * (kl - 2);
+      if (h < min_n) { ubd = d - 1; break; }
+    }
+  }
+  return ubd;
+}
+
+
+// ---- kernel parameter blocks and entry points ----
+struct PrepJob {
+  uint32_t slot, q, kl, ubd;
+  uint32_t l, h, limit_doms, rules;
+  uint32_t kl_heu, root_to_pool, pad0, pad1;
+  unsigned long long node_budget;
+};
+
+struct PrepScratch {
+  uint16_t *dist;  // [jobs][n]
+  uint32_t *vis;   // [jobs][nw]
+  uint32_t *comp;  // [jobs][nw]
+  uint32_t *fa;    // [jobs][n]
+  uint32_t *fb;    // [jobs][n]
+  uint32_t *wpre;  // [jobs][nw+1]
+  uint32_t stride_n;
+  uint32_t stride_w;
+};
+
+struct SearchParams {
+  DevGraph g;
+  SlotArrays sa;
+  Slot *slots;
+  Pool pool;
+  Counters *ctr;
+  Stacks stk;
+  Scratch scr;
+  uint32_t nw_smem;                 // state words that fit in shared memory
+  unsigned long long slice_ns;      // slice length (device clock)
+  // test mode (one step per CTA)
+  const uint32_t *t_rec;            // input records
+  const unsigned long long *t_rec_off;
+  uint32_t t_ntasks;
+  uint32_t *t_hdr;                  // 16 per task
+  uint32_t *t_doms;
+  uint32_t t_doms_stride;
+  uint32_t *t_kids;
+  unsigned long long t_kids_stride;
+  uint32_t *t_wit;
+  uint32_t t_wit_stride;
+  const uint32_t *t_kl;             // incumbent per test task
+};
+
+constexpr int PREP_THREADS = 512;
+constexpr int SEARCH_THREADS = 512;
+
+__global__ void prep_kernel(DevGraph g, SlotArrays sa, Slot *slots,
+                            const PrepJob *jobs, int njobs, PrepScratch ps,
+                            Pool pool, Counters *ctr);
+__global__ void search_kernel(SearchParams P);
+__global__ void step_test_kernel(SearchParams P);
+size_t search_static_smem();
+
+}  // namespace scs

@@ -1,0 +1,196 @@
+"""GPU parity tests: the CUDA path (through the C ABI) against the CPU oracle.
+
+* preprocessing: the local graph built on the GPU equals orc_prepare's
+  (bit-exact: local ids, CSR, distances);
+* one branch-and-bound step: header, bounds, ustar, dominated vertices,
+  children (entries bit-exact, degrees equal to a recount) and witness equal
+  orc_step's on tasks of the oracle's own search;
+* whole searches: the reported maximum minimum degree equals brute force on
+  small graphs and the oracle's exact answers on the 4000-vertex Chung-Lu
+  workload; every returned community is verified.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import random_graph
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _engine(**kw):
+    from scs_gb300.engine import Engine
+    kw.setdefault("pool_words", 1 << 26)
+    kw.setdefault("stack_words", 1 << 22)
+    kw.setdefault("slice_us", 50000)
+    return Engine(**kw)
+
+
+@pytest.fixture(scope="module")
+def og_c1(chunglu_small, oracle_lib):
+    return oracle_lib.OracleGraph.from_file(chunglu_small)
+
+
+@pytest.fixture(scope="module")
+def eng_c1(chunglu_small):
+    e = _engine(graph=chunglu_small, limit_queries=64)
+    yield e
+    e.close()
+
+
+def _queries_c1(og):
+    from scs_gb300 import workloads as W
+    return W.queries_small(og.core)
+
+
+def _prep_cases(og, oracle, count):
+    out = []
+    for (l, h, q, hf, ld) in _queries_c1(og)[:count].tolist():
+        kl, _ = og.heuristic(0, l, h, q)
+        ku = min(int(og.core[q]), h - 1)
+        if kl >= ku:
+            continue
+        out.append((l, h, q, ld, kl, int(oracle.lib().orc_ubd_host(kl, h))))
+    return out
+
+
+def test_prepare_parity(eng_c1, og_c1, oracle_lib):
+    cases = _prep_cases(og_c1, oracle_lib, 24)
+    assert len(cases) >= 10
+    qs = [(l, h, q, 0, ld) for (l, h, q, ld, kl, ubd) in cases]
+    nl, ql = eng_c1.debug_prepare(qs, [c[4] for c in cases], [c[5] for c in cases])
+    for i, (l, h, q, ld, kl, ubd) in enumerate(cases):
+        ctx = oracle_lib.OracleCtx(og_c1, l, h, q, kl, ubd, ld)
+        assert int(nl[i]) == ctx.n and int(ql[i]) == ctx.q_local
+        gid, off, adj, dist = eng_c1.debug_local_graph(i, int(nl[i]), int(ctx.off[-1]) + 8)
+        assert np.array_equal(gid, ctx.gid)
+        assert np.array_equal(off, ctx.off)
+        assert np.array_equal(adj, ctx.adj)
+        assert np.array_equal(dist, ctx.dist)
+
+
+def _compare_steps(eng, ctxs, tasks):
+    """tasks: list of (slot, kl, entries); ctxs: slot -> OracleCtx."""
+    got = eng.debug_step(tasks)
+    for (slot, kl, ent), g in zip(tasks, got):
+        ctx = ctxs[slot]
+        r = ctx.step(ent, kl)
+        h, gh = r["hdr"], g["hdr"]
+        for f in (0, 1, 2, 3, 5, 6, 7, 8, 11):
+            assert int(h[f]) == int(gh[f]), ("hdr", f, list(h), list(gh))
+        if h[0] in (0, 2, 3):
+            assert int(h[4]) == int(gh[4])
+        assert np.array_equal(r["doms"], g["doms"])
+        if r["wit"] is not None:
+            assert np.array_equal(r["wit"], g["wit"])
+        assert len(r["kids"]) == len(g["kids"])
+        for (s1, c1, e1), (s2, c2, e2, d2) in zip(r["kids"], g["kids"]):
+            assert (s1, c1) == (s2, c2)
+            assert np.array_equal(e1, e2)
+            dc, dr = ctx.degrees(e2)
+            assert np.array_equal(d2 >> 16, dc) and np.array_equal(d2 & 0xFFFF, dr)
+    return got
+
+
+def test_step_parity_search_tasks(eng_c1, og_c1, oracle_lib):
+    cases = _prep_cases(og_c1, oracle_lib, 12)[:6]
+    qs = [(l, h, q, 0, ld) for (l, h, q, ld, kl, ubd) in cases]
+    eng_c1.debug_prepare(qs, [c[4] for c in cases], [c[5] for c in cases])
+    ctxs, tasks = {}, []
+    for i, (l, h, q, ld, kl, ubd) in enumerate(cases):
+        ctxs[i] = oracle_lib.OracleCtx(og_c1, l, h, q, kl, ubd, ld)
+        for e, k in ctxs[i].collect_tasks(kl, 40):
+            tasks.append((i, k, e))
+            tasks.append((i, k + 1, e))  # a tighter incumbent exercises pruning
+    assert len(tasks) >= 200
+    got = _compare_steps(eng_c1, ctxs, tasks)
+    outcomes = {int(g["hdr"][0]) for g in got}
+    assert 0 in outcomes and len(outcomes) >= 2
+
+
+def test_step_parity_random_graphs(oracle_lib):
+    """Dense small graphs with rule-3 promotions, dominated vertices and all
+    rule subsets."""
+    rng = np.random.default_rng(5)
+    for trial in range(3):
+        n, off, adj = random_graph(rng, 60, 0.25 + 0.1 * trial)
+        og = oracle_lib.OracleGraph(n, off, adj)
+        for rules in ((1, 1, 1, 1, 1), (1, 0, 1, 0, 1), (0, 1, 0, 1, 0)):
+            eng = _engine(csr=(n, off, adj), limit_queries=8, rules=rules)
+            rb = sum(b << i for i, b in enumerate(rules))
+            cases = []
+            for q in range(0, n, 9)[:6]:
+                l, h = 3, 9
+                cases.append((l, h, q, 10, 1, int(oracle_lib.lib().orc_ubd_host(1, h))))
+            qs = [(l, h, q, 0, ld) for (l, h, q, ld, kl, ubd) in cases]
+            eng.debug_prepare(qs, [c[4] for c in cases], [c[5] for c in cases])
+            ctxs, tasks = {}, []
+            for i, (l, h, q, ld, kl, ubd) in enumerate(cases):
+                ctxs[i] = oracle_lib.OracleCtx(og, l, h, q, kl, ubd, ld, rules=rb)
+                for e, k in ctxs[i].collect_tasks(kl, 25):
+                    tasks.append((i, k, e))
+            _compare_steps(eng, ctxs, tasks)
+            eng.close()
+
+
+def test_search_vs_bruteforce():
+    """Disjoint union of small random graphs; every answer equals the
+    exhaustive optimum (heuristic off) or max(optimum, greedy kl)."""
+    import oracle as O
+    from scs_gb300 import workloads as W
+    cases = json.load(open(os.path.join(GOLD, "bruteforce_small.json")))
+    us, vs, base, rows, want = [], [], 0, [], []
+    for c in cases:
+        us.append(np.array(c["u"], dtype=np.int64) + base)
+        vs.append(np.array(c["v"], dtype=np.int64) + base)
+        for qq in c["queries"]:
+            rows.append((qq["l"], qq["h"], qq["q"] + base))
+            want.append(qq["degree"])
+        base += c["n"]
+    off, adj = W.to_csr(base, np.concatenate(us).astype(np.uint32),
+                        np.concatenate(vs).astype(np.uint32))
+    og = O.OracleGraph(base, off, adj)
+    eng = _engine(csr=(base, off, adj), limit_queries=128)
+    res0 = eng.solve([(l, h, q, 0, 10) for (l, h, q) in rows])
+    res1 = eng.solve([(l, h, q, 1, 10) for (l, h, q) in rows])
+    for (l, h, q), w, r0, r1 in zip(rows, want, res0, res1):
+        assert r0["degree"] == w, (l, h, q, w, r0)
+        kl, _ = og.heuristic(0, l, h, q)
+        assert r1["kl_heuristic"] == kl
+        assert r1["degree"] == max(w, kl), (l, h, q, w, kl, r1)
+        if r0["degree"] > 0:
+            assert r0["h_verified"] == 1, r0
+    eng.close()
+
+
+def test_search_chunglu_golden(eng_c1, og_c1):
+    """All 50 queries of the 4000-vertex Chung-Lu workload against the
+    oracle's exact answers."""
+    from oracle import verify_community
+    gold = json.load(open(os.path.join(GOLD, "answers_chunglu_n4000.json")))
+    rows = [(g["l"], g["h"], g["q"], g["heur"], g["limit_doms"]) for g in gold["queries"]]
+    res = eng_c1.solve(rows)
+    checked = 0
+    for g, r in zip(gold["queries"], res):
+        assert r["status"] in (0, 1), r
+        assert r["kl_heuristic"] == g["kl_heu"]
+        if g["finished"]:
+            assert r["degree"] == g["degree"], (g, r)
+            checked += 1
+        c, hq, sz, md = verify_community(og_c1, r["H"], g["q"], g["l"], g["h"])
+        if r["h_verified"]:
+            assert c and hq and sz and md == r["degree"]
+    assert checked >= 40
+
+
+def test_results_same_alone_and_in_mix(eng_c1, og_c1):
+    """A query's answer does not depend on what else runs with it."""
+    rows = [tuple(int(x) for x in r) for r in _queries_c1(og_c1)[:12]]
+    mix = eng_c1.solve(rows)
+    for row, m in zip(rows[:4], mix[:4]):
+        alone = eng_c1.solve([row])[0]
+        assert alone["degree"] == m["degree"]
+        assert alone["status"] == m["status"]
