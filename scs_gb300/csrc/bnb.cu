@@ -1032,6 +1032,31 @@ __device__ bool publish_pool(const SearchParams &P, unsigned long long off) {
   return true;
 }
 
+// Header sanity of a task record (thread 0): slot in range and searching,
+// 1 <= s <= n_local, csize <= s, len == 2s+5, footer == len, entry ids in
+// range and ascending.  Returns 0 or a code naming the first failed check.
+__device__ uint32_t check_record(const SearchParams &P, const uint32_t *rec,
+                                 int from_pool) {
+  uint32_t slot = rec[0], s = rec[1], cs = rec[2], len = rec[3];
+  if (slot >= P.nslots) return 1;
+  const Slot *sl = P.slots + slot;
+  if (*(const volatile uint32_t *)&sl->state != SLOT_SEARCH) return 2;
+  uint32_t nl = *(const volatile uint32_t *)&sl->n_local;
+  if (s == 0 || s > nl) return 3;
+  if (cs > s) return 4;
+  if (len != 2 * s + 5) return 5;
+  if (rec[REC_HDR + 2 * s] != len) return 6;
+  uint32_t prev = 0;
+  for (uint32_t i = 0; i < s; i++) {
+    uint32_t id = rec[REC_HDR + i] >> 1;
+    if (id >= nl) return 7;
+    if (i && id <= prev) return 8;
+    prev = id;
+  }
+  (void)from_pool;
+  return 0;
+}
+
 // claim one pool record; returns arena offset+1 or 0
 __device__ unsigned long long pool_take(const SearchParams &P) {
   for (int attempt = 0; attempt < 64; attempt++) {
@@ -1123,9 +1148,24 @@ search_kernel(SearchParams P) {
       if (sh.stop) break;
       if (!s_rec) continue;
       const uint32_t *rec = s_rec;
+      if (t == 0) {
+        // validate the record before trusting any index in it
+        uint32_t bad = check_record(P, rec, s_pool_rec);
+        if (bad) {
+          atomicOr(&P.ctr->error, ERR_RECORD);
+          P.ctr->err_info[0] = bad;
+          P.ctr->err_info[1] = rec[0];
+          P.ctr->err_info[2] = rec[1];
+          P.ctr->err_info[3] = rec[3];
+          sh.stop = 1;
+        }
+      }
+      __syncthreads();
+      if (sh.stop) break;
       set_task_header(P, sh, rec);
-      Slot *sl = P.slots + sh.slot;
-      if (*(volatile uint32_t *)&sl->abort) {
+      if (t == 0) sh.wit_pending = *(volatile uint32_t *)&P.slots[sh.slot].abort;
+      __syncthreads();
+      if (sh.wit_pending) {
         if (t == 0) finish_tasks(P, sh.slot, -1);
         __syncthreads();
         continue;
@@ -1166,7 +1206,10 @@ search_kernel(SearchParams P) {
           }
         }
         __syncthreads();
-        if (!s_rec) continue;
+        if (!s_rec) {
+          __syncthreads();
+          continue;
+        }
         {
           uint32_t *r = s_rec;
           write_child(T, sh, (uint32_t)code, r + REC_HDR, r + REC_HDR + s2, r);

@@ -252,6 +252,7 @@ static SearchParams make_params(scs_engine *E) {
   P.stk = E->stk;
   P.scr = E->scr;
   P.nw_smem = E->nw_smem;
+  P.nslots = E->nslots;
   return P;
 }
 
@@ -424,7 +425,11 @@ static int slice(scs_engine *E) {
   E->stats[SCS_STAT_SPILLS] = hc.spills;
   E->stats[SCS_STAT_PREP_BYTES] = hc.prep_bytes;
   if (hc.error) {
-    E->err = "device error flags " + std::to_string(hc.error);
+    E->err = "device error flags " + std::to_string(hc.error) + " info " +
+             std::to_string(hc.err_info[0]) + "," + std::to_string(hc.err_info[1]) + "," +
+             std::to_string(hc.err_info[2]) + "," + std::to_string(hc.err_info[3]);
+    fprintf(stderr, "scs: %s\n", E->err.c_str());
+    if (hc.error & (ERR_RECORD | ERR_SPIN)) return SCS_ECUDA;
     E->stats[SCS_STAT_COUNT - 1] |= hc.error;
   }
   // collect finished slots

@@ -172,6 +172,7 @@ struct SearchParams {
   Stacks stk;
   Scratch scr;
   uint32_t nw_smem;                 // state words that fit in shared memory
+  uint32_t nslots;
   unsigned long long slice_ns;      // slice length (device clock)
   // test mode (one step per CTA)
   const uint32_t *t_rec;            // input records
