@@ -171,7 +171,9 @@ __device__ void load_record(const uint32_t *rec, Task &T, Sh &sh) {
   if (t == 0) sh.cnt[0] = 0;
   __syncthreads();
   for (uint32_t i = t; i < s; i += BT) {
-    uint32_t e = ent[i], dg = deg[i];
+    // records may have been written by another SM: read through L2 so no
+    // stale L1 line of an earlier neighbour in the arena is used
+    uint32_t e = __ldcg(ent + i), dg = __ldcg(deg + i);
     uint32_t id = e >> 1, c = e & 1u;
     T.W[id] = ((c ? ST_C : ST_R) << 30) | ((dg >> 16) << 15) | (dg & 0xFFFFu);
     T.list[i] = id;
@@ -903,9 +905,9 @@ __device__ Task make_task(const SearchParams &P, Sh &sh, uint32_t *dyn,
 __device__ void set_task_header(const SearchParams &P, Sh &sh,
                                 const uint32_t *rec) {
   if (threadIdx.x == 0) {
-    sh.slot = rec[0];
-    sh.s = rec[1];
-    sh.csize = rec[2];
+    sh.slot = __ldcg(rec);
+    sh.s = __ldcg(rec + 1);
+    sh.csize = __ldcg(rec + 2);
     Slot *sl = P.slots + sh.slot;
     sh.n_local = sl->n_local;
     sh.l = sl->l;
@@ -1037,7 +1039,8 @@ __device__ bool publish_pool(const SearchParams &P, unsigned long long off) {
 // range and ascending.  Returns 0 or a code naming the first failed check.
 __device__ uint32_t check_record(const SearchParams &P, const uint32_t *rec,
                                  int from_pool) {
-  uint32_t slot = rec[0], s = rec[1], cs = rec[2], len = rec[3];
+  uint32_t slot = __ldcg(rec), s = __ldcg(rec + 1), cs = __ldcg(rec + 2),
+           len = __ldcg(rec + 3);
   if (slot >= P.nslots) return 1;
   const Slot *sl = P.slots + slot;
   if (*(const volatile uint32_t *)&sl->state != SLOT_SEARCH) return 2;
@@ -1045,10 +1048,10 @@ __device__ uint32_t check_record(const SearchParams &P, const uint32_t *rec,
   if (s == 0 || s > nl) return 3;
   if (cs > s) return 4;
   if (len != 2 * s + 5) return 5;
-  if (rec[REC_HDR + 2 * s] != len) return 6;
+  if (__ldcg(rec + REC_HDR + 2 * s) != len) return 6;
   uint32_t prev = 0;
   for (uint32_t i = 0; i < s; i++) {
-    uint32_t id = rec[REC_HDR + i] >> 1;
+    uint32_t id = __ldcg(rec + REC_HDR + i) >> 1;
     if (id >= nl) return 7;
     if (i && id <= prev) return 8;
     prev = id;
@@ -1110,7 +1113,7 @@ search_kernel(SearchParams P) {
         s_rec = nullptr;
         s_pool_rec = 0;
         if (s_top > s_bot) {
-          uint32_t len = sbase[s_top - 1];
+          uint32_t len = __ldcg(sbase + s_top - 1);
           if (len < 5 || len > s_top - s_bot) {
             atomicOr(&P.ctr->error, ERR_RECORD);
             s_top = s_bot;
@@ -1244,7 +1247,7 @@ search_kernel(SearchParams P) {
     if (t == 0) {
       s_rec = nullptr;
       if (*(volatile uint32_t *)&P.ctr->hungry > 0 && s_top > s_bot) {
-        uint32_t len = sbase[s_bot + 3];
+        uint32_t len = __ldcg(sbase + s_bot + 3);
         if (len >= 5 && s_bot + len < s_top) {  // keep at least one record
           unsigned long long off = atomicAdd(P.pool.arena_top, (unsigned long long)len);
           if (off + len <= P.pool.arena_cap) {
@@ -1257,8 +1260,8 @@ search_kernel(SearchParams P) {
     __syncthreads();
     if (s_rec) {
       const uint32_t *src = sbase + s_bot;
-      const uint32_t len = src[3];
-      for (uint32_t i = t; i < len; i += BT) s_rec[i] = src[i];
+      const uint32_t len = __ldcg(src + 3);
+      for (uint32_t i = t; i < len; i += BT) s_rec[i] = __ldcg(src + i);
       __syncthreads();
       if (t == 0) {
         if (publish_pool(P, s_pool_off)) {
