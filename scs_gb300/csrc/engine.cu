@@ -401,6 +401,9 @@ static int slice(scs_engine *E) {
   // done_count, stop
   CK(cudaMemsetAsync(&E->d_ctr->deadline, 0, 8, E->stream));
   CK(cudaMemsetAsync(&E->d_ctr->hungry, 0, sizeof(uint32_t) * 4, E->stream));
+  // the dynamic shared-memory limit is per function, not per engine
+  CK(cudaFuncSetAttribute(search_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                          (int)E->smem_bytes));
   CK(cudaEventRecord(E->ev0, E->stream));
   search_kernel<<<E->grid, SEARCH_THREADS, E->smem_bytes, E->stream>>>(P);
   CK(cudaGetLastError());
@@ -772,6 +775,8 @@ int scs_debug_step(scs_engine *E, uint32_t ntasks, const uint32_t *task_slot,
     P.t_wit = d_wit;
     P.t_wit_stride = wit_stride;
     P.t_kl = d_kl + base;
+    cudaFuncSetAttribute(step_test_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)E->smem_bytes);
     step_test_kernel<<<cnt, SEARCH_THREADS, E->smem_bytes, E->stream>>>(P);
     cudaError_t e = cudaStreamSynchronize(E->stream);
     if (e == cudaSuccess) e = cudaGetLastError();
