@@ -844,11 +844,20 @@ int orc_solve(const orc_graph *g, uint32_t l, uint32_t h, uint32_t q,
               uint32_t heur, uint32_t limit_doms, uint32_t rules,
               uint64_t node_limit, orc_result *res, uint32_t *H,
               uint32_t h_cap) {
+  return orc_solve_from(g, l, h, q, heur, limit_doms, rules, node_limit, 0,
+                        res, H, h_cap);
+}
+
+int orc_solve_from(const orc_graph *g, uint32_t l, uint32_t h, uint32_t q,
+                   uint32_t heur, uint32_t limit_doms, uint32_t rules,
+                   uint64_t node_limit, uint32_t kl_floor, orc_result *res,
+                   uint32_t *H, uint32_t h_cap) {
   memset(res, 0, sizeof(*res));
   uint32_t ku = g->core[q] < h - 1 ? g->core[q] : h - 1;
   uint32_t kl = 0, hs = 0;
   uint32_t *Hh = (uint32_t *)malloc((g->n ? g->n : 1) * sizeof(uint32_t));
   if (heur) kl = orc_cssc_heu(g, l, h, q, Hh, &hs);
+  if (kl_floor > kl) kl = kl_floor; /* a known lower bound (proof-only runs) */
   res->kl_heu = kl;
   res->ku = ku;
   if (kl == ku) {

@@ -86,6 +86,14 @@ int orc_solve(const orc_graph *g, uint32_t l, uint32_t h, uint32_t q,
               uint64_t node_limit, orc_result *res, uint32_t *H,
               uint32_t h_cap);
 
+/* As orc_solve, with the incumbent raised to at least kl_floor before the
+ * search (measures the proof part of a search when kl_floor is the optimum;
+ * the result is then max(optimum, kl_floor)). */
+int orc_solve_from(const orc_graph *g, uint32_t l, uint32_t h, uint32_t q,
+                   uint32_t heur, uint32_t limit_doms, uint32_t rules,
+                   uint64_t node_limit, uint32_t kl_floor, orc_result *res,
+                   uint32_t *H, uint32_t h_cap);
+
 /* Exhaustive solver for small components: max over connected S containing q
  * with l <= |S| <= h of min degree (0 if none).  Returns UINT32_MAX when the
  * component of q has more than `max_comp` vertices. */

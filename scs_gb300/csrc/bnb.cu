@@ -925,7 +925,7 @@ __device__ void set_task_header(const SearchParams &P, Sh &sh,
 // test entry: one deterministic step per CTA, all children written in
 // canonical order Include, Dom_0..Dom_{k-1}, Exclude (dead ones skipped)
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(BT, 1)
+__global__ void __launch_bounds__(BT, 6)
 step_test_kernel(SearchParams P) {
   extern __shared__ uint32_t dyn[];
   __shared__ Sh sh;
@@ -1079,7 +1079,7 @@ __device__ unsigned long long pool_take(const SearchParams &P) {
   return 0;
 }
 
-__global__ void __launch_bounds__(BT, 1)
+__global__ void __launch_bounds__(BT, 6)
 search_kernel(SearchParams P) {
   extern __shared__ uint32_t dyn[];
   __shared__ Sh sh;

@@ -181,10 +181,12 @@ static int engine_init(scs_engine *E) {
   // search grid and shared memory
   int max_optin = 0;
   CK(cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, E->dev));
-  uint32_t cps = c.ctas_per_sm ? c.ctas_per_sm : 1;
+  // CTAs per SM: several small CTAs keep several tasks in flight per SM so
+  // one task's serial phases overlap with the others' work
+  uint32_t cps = c.ctas_per_sm ? c.ctas_per_sm : 6;
   size_t stat = search_static_smem();
-  size_t budget = (size_t)max_optin;
-  if (cps > 1) budget = std::min(budget, (size_t)(228 * 1024) / cps - 1024);
+  size_t per_sm = 228 * 1024;
+  size_t budget = std::min((size_t)max_optin, per_sm / cps - 1024);
   size_t words = budget > stat ? (budget - stat) / 4 : 0;
   E->nw_smem = (uint32_t)std::min<size_t>(words, std::min<uint32_t>(n, MAX_LOCAL));
   E->smem_bytes = (size_t)E->nw_smem * 4;
@@ -215,7 +217,7 @@ static int engine_init(scs_engine *E) {
   uint64_t sw = c.stack_words;
   if (!sw) {
     // a few hundred root-sized records per CTA, capped by 40% of free memory
-    uint64_t want = std::max<uint64_t>(1ull << 20, (uint64_t)(2 * n + 5) * 256);
+    uint64_t want = std::max<uint64_t>(1ull << 20, (uint64_t)(2 * n + 5) * 64);
     uint64_t cap = (uint64_t)(free_b * 0.4) / 4 / E->grid;
     sw = std::min(want, cap);
   }

@@ -189,7 +189,7 @@ struct SearchParams {
 };
 
 constexpr int PREP_THREADS = 512;
-constexpr int SEARCH_THREADS = 512;
+constexpr int SEARCH_THREADS = 128;
 
 __global__ void prep_kernel(DevGraph g, SlotArrays sa, Slot *slots,
                             const PrepJob *jobs, int njobs, PrepScratch ps,

@@ -137,6 +137,6 @@ if __name__ == "__main__":
     if what in ("brute", "all"):
         make_brute()
     if what in ("answers", "all"):
-        make_answers(tmp, "chunglu_n4000", 50, 0, 8)
+        make_answers(tmp, "chunglu_n4000", 50, 300000, 8)
     if what == "answers_rmat":
         make_answers(tmp, "rmat_s15_ef16", int(sys.argv[2]), int(sys.argv[3]), 8)
