@@ -49,7 +49,6 @@ struct Sh {
   uint32_t A[CL_CAP];
   uint32_t B[CL_CAP];
   uint32_t hist[CL_CAP + 1];
-  double wsum[NWARP][32];
   uint32_t kid_len[MAX_DOMS + 2];
   unsigned long long kid_dst[MAX_DOMS + 2];
 };
@@ -151,7 +150,9 @@ struct Task {
   uint32_t *list;
   uint32_t *aux;
   uint32_t *tmp;
-  double *dsc;
+  double *ssc;   // pushed ustar scores, by local id (zero between uses)
+  double *dsc;   // pushed dom-score partial sums, by local id
+  double *dsc2;  // scores of dominated candidates, by position
   const uint32_t *off;
   const uint32_t *adj;
   const uint16_t *dist;
@@ -463,52 +464,45 @@ __device__ void bounds(Task &T, Sh &sh) {
   __syncthreads();
 }
 
-// ordered sum of 1/dC over C neighbours of x (ascending neighbour order);
-// zero_dc_weight: term used when dC == 0 (1.0 for ustar, 0.0 for doms).
-// When `dom_check`, also tests that every live neighbour is marked in aux.
-__device__ double warp_score(Task &T, Sh &sh, uint32_t x, double zero_w,
-                             bool dom_check, bool &dominated) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  double total = 0.0;
-  dominated = true;
-  uint32_t b = T.off[x], e = T.off[x + 1];
-  for (uint32_t k = b; k < e; k += 32) {
-    double term = 0.0;
-    bool bad = false;
-    if (k + lane < e) {
-      uint32_t nb = T.adj[k + lane];
-      if (nb != SENT) {
-        uint32_t w = T.W[nb];
-        if (dom_check && live(w) && T.aux[nb] == 0u) bad = true;
-        if (st_of(w) == ST_C) {
-          uint32_t dc = dc_of(w);
-          term = dc ? __ddiv_rn(1.0, (double)dc) : zero_w;
-        }
-      }
-    }
-    if (dom_check && __any_sync(0xffffffffu, bad)) {
-      dominated = false;
-      return 0.0;
-    }
-    unsigned m = __ballot_sync(0xffffffffu, term != 0.0);
-    if (m) {
-      if (term != 0.0) sh.wsum[wid][__popc(m & ((1u << lane) - 1u))] = term;
-      __syncwarp();
-      if (lane == 0) {
-        int c = __popc(m);
-        for (int j = 0; j < c; j++) total = __dadd_rn(total, sh.wsum[wid][j]);
-      }
-      __syncwarp();
-    }
-  }
-  return __shfl_sync(0xffffffffu, total, 0);
-}
-
 // ---------------------------------------------------------------------------
 // ustar (src/helpers.cc:1104-1168) and dominated vertices (:545-670)
+//
+// Scores are pushed from C: for each u in C in ascending id order, every R
+// neighbour v gets += 1/dC(u) (1.0 when dC(u) == 0) into ssc[v] and
+// += 1/dC(u) (0.0 when dC(u) == 0) into dsc[v].  Each v receives its terms in
+// ascending u order -- the order the oracle sums them scanning N(v) -- so the
+// doubles are bit-identical, and the work is sum deg(C) instead of
+// sum deg(candidates).
 // ---------------------------------------------------------------------------
+__device__ void score_candidates(Task &T, Sh &sh) {
+  const int t = threadIdx.x;
+  const uint32_t cs = min(sh.csize, (uint32_t)CL_CAP);
+  // C in ascending id order (rank sort into sh.A)
+  for (uint32_t i = t; i < cs; i += BT) {
+    uint32_t vi = sh.cl[i], r = 0;
+    for (uint32_t j = 0; j < cs; j++) r += sh.cl[j] < vi;
+    sh.A[r] = vi;
+  }
+  __syncthreads();
+  for (uint32_t ci = 0; ci < cs; ci++) {
+    const uint32_t u = sh.A[ci];
+    const uint32_t dc = dc_of(T.W[u]);
+    const double wu = dc ? __ddiv_rn(1.0, (double)dc) : 1.0;
+    const double wd = dc ? wu : 0.0;
+    const uint32_t b = T.off[u], e = T.off[u + 1];
+    for (uint32_t k = b + t; k < e; k += BT) {
+      uint32_t nb = T.adj[k];
+      if (nb != SENT && st_of(T.W[nb]) == ST_R) {
+        T.ssc[nb] = __dadd_rn(T.ssc[nb], wu);
+        T.dsc[nb] = __dadd_rn(T.dsc[nb], wd);
+      }
+    }
+    __syncthreads();
+  }
+}
+
 __device__ void choose_ustar(Task &T, Sh &sh) {
-  const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+  const int t = threadIdx.x;
   const uint32_t s = sh.s;
   if (t == 0) sh.cnt[0] = 0;
   __syncthreads();
@@ -525,22 +519,18 @@ __device__ void choose_ustar(Task &T, Sh &sh) {
   }
   __syncthreads();
   const uint32_t nc = sh.cnt[0];
+  score_candidates(T, sh);
   const double dmax = (double)sh.dmax;
   double best = 0.0;
   uint32_t bid = UINT32_MAX;
-  for (uint32_t ci = wid; ci < nc; ci += NWARP) {
+  for (uint32_t ci = t; ci < nc; ci += BT) {
     uint32_t x = T.tmp[ci];
-    bool dummy;
-    double sc = warp_score(T, sh, x, 1.0, false, dummy);
+    double sc = T.ssc[x];
     if (sc > 0.0) sc = __dadd_rn(sc, __ddiv_rn((double)dr_of(T.W[x]), dmax));
     if (sc > best || (sc == best && sc > 0.0 && x < bid)) {
       best = sc;
       bid = x;
     }
-  }
-  if (lane != 0) {
-    best = 0.0;
-    bid = UINT32_MAX;
   }
   double osc;
   uint32_t oid;
@@ -548,6 +538,17 @@ __device__ void choose_ustar(Task &T, Sh &sh) {
   if (t == 0) {
     sh.ustar = (osc > 0.0) ? oid : UINT32_MAX;
     sh.ndom_cand = nc;
+  }
+  __syncthreads();
+}
+
+// reset the pushed scores (candidates are exactly the R vertices with C
+// neighbours, i.e. every vertex that received a term)
+__device__ void clear_scores(Task &T, Sh &sh) {
+  for (uint32_t ci = threadIdx.x; ci < sh.ndom_cand; ci += BT) {
+    uint32_t x = T.tmp[ci];
+    T.ssc[x] = 0.0;
+    T.dsc[x] = 0.0;
   }
   __syncthreads();
 }
@@ -562,6 +563,21 @@ __device__ uint32_t list_index(const uint32_t *list, uint32_t s, uint32_t x) {
   return lo;
 }
 
+// every live neighbour of x is u* or a neighbour of u* (marked in aux)
+__device__ bool warp_dominated(Task &T, uint32_t x) {
+  const int lane = threadIdx.x & 31;
+  uint32_t b = T.off[x], e = T.off[x + 1];
+  for (uint32_t k = b; k < e; k += 32) {
+    bool bad = false;
+    if (k + lane < e) {
+      uint32_t nb = T.adj[k + lane];
+      if (nb != SENT && live(T.W[nb]) && T.aux[nb] == 0u) bad = true;
+    }
+    if (__any_sync(0xffffffffu, bad)) return false;
+  }
+  return true;
+}
+
 __device__ void find_doms(Task &T, Sh &sh) {
   const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
   const uint32_t u = sh.ustar;
@@ -571,6 +587,8 @@ __device__ void find_doms(Task &T, Sh &sh) {
   }
   __syncthreads();
   if (sh.ldoms == 0) return;
+  const uint32_t wu = T.W[u];
+  const uint32_t degu = dc_of(wu) + dr_of(wu), dcu = dc_of(wu);
   // mark N_T(u*) and u*
   {
     uint32_t b = T.off[u], e = T.off[u + 1];
@@ -581,22 +599,21 @@ __device__ void find_doms(Task &T, Sh &sh) {
     if (t == 0) T.aux[u] = 1u;
   }
   __syncthreads();
-  // candidates were collected by choose_ustar in tmp[0..nc): R with dC > 0
+  // candidates (R, dC > 0) are in tmp[0..nc); necessary conditions for
+  // N_T(v) within N_T(u*)+u*: dC(v) <= dC(u*), deg_T(v) <= deg_T(u*) + 1
   const uint32_t nc = sh.ndom_cand;
   const double dmax = (double)sh.dmax;
   uint32_t *dom_id = T.tmp + sh.s;  // second half of tmp (s <= n)
   for (uint32_t ci = wid; ci < nc; ci += NWARP) {
     uint32_t x = T.tmp[ci];
     if (x == u) continue;
-    bool dom;
-    double sc = warp_score(T, sh, x, 0.0, true, dom);
-    if (dom) {
-      sc = __dadd_rn(sc, __ddiv_rn((double)dr_of(T.W[x]), dmax));
-      if (lane == 0) {
-        uint32_t k = atomicAdd(&sh.cnt[1], 1u);
-        dom_id[k] = x;
-        T.dsc[k] = sc;
-      }
+    uint32_t wx = T.W[x];
+    if (dc_of(wx) > dcu || dc_of(wx) + dr_of(wx) > degu + 1u) continue;
+    if (warp_dominated(T, x) && lane == 0) {
+      double sc = __dadd_rn(T.dsc[x], __ddiv_rn((double)dr_of(wx), dmax));
+      uint32_t k = atomicAdd(&sh.cnt[1], 1u);
+      dom_id[k] = x;
+      T.dsc2[k] = sc;
     }
   }
   __syncthreads();
@@ -616,7 +633,7 @@ __device__ void find_doms(Task &T, Sh &sh) {
     double bs = -1.0;
     uint32_t bi = UINT32_MAX, bpos = UINT32_MAX;
     for (uint32_t i = t; i < nd; i += BT) {
-      double sc = T.dsc[i];
+      double sc = T.dsc2[i];
       uint32_t x = dom_id[i];
       if (sc > bs || (sc == bs && x < bi)) {
         bs = sc;
@@ -628,7 +645,7 @@ __device__ void find_doms(Task &T, Sh &sh) {
     uint32_t oid;
     block_argmax(bs, bi, sh, osc, oid);
     if (bi == oid && bpos != UINT32_MAX && bs == osc) {
-      T.dsc[bpos] = -2.0;  // exclude from later rounds
+      T.dsc2[bpos] = -2.0;  // exclude from later rounds
       sh.doms[r] = oid;
     }
     __syncthreads();
@@ -875,11 +892,13 @@ __device__ void step_core(Task &T, Sh &sh, bool test, uint32_t *t_wit) {
   }
   choose_ustar(T, sh);
   if (sh.ustar == UINT32_MAX) {
+    clear_scores(T, sh);
     if (t == 0) sh.outcome = 3;
     __syncthreads();
     return;
   }
   find_doms(T, sh);
+  clear_scores(T, sh);
   mark_children(T, sh);
 }
 
@@ -892,7 +911,9 @@ __device__ Task make_task(const SearchParams &P, Sh &sh, uint32_t *dyn,
   T.list = P.scr.list + (size_t)cta * st;
   T.aux = P.scr.aux + (size_t)cta * st;
   T.tmp = P.scr.tmp + (size_t)cta * 2 * st;
-  T.dsc = P.scr.dsc + (size_t)cta * st;
+  T.ssc = P.scr.dsc + (size_t)cta * 3 * st;
+  T.dsc = T.ssc + st;
+  T.dsc2 = T.dsc + st;
   T.off = P.sa.loc_off + (size_t)slot * (P.sa.stride_n + 1);
   T.adj = P.sa.loc_adj + (size_t)slot * P.sa.cap_adj;
   T.dist = P.sa.loc_dist + (size_t)slot * P.sa.stride_n;
@@ -1079,6 +1100,30 @@ __device__ unsigned long long pool_take(const SearchParams &P) {
   return 0;
 }
 
+// When a record of `len` words would not fit above `top` but the stack has
+// room below `bot` (left by donations), slide [bot, top) down to 0.  All
+// threads call this; the copy runs in chunks no longer than the shift so no
+// chunk overlaps its own destination.
+__device__ void stack_make_room(const SearchParams &P, uint32_t *sbase,
+                                uint32_t len, unsigned long long &top,
+                                unsigned long long &bot) {
+  unsigned long long t0 = top, b0 = bot;
+  if (t0 + len <= P.stk.words || b0 == 0) return;
+  const unsigned long long used = t0 - b0, shift = b0;
+  for (unsigned long long base = 0; base < used; base += shift) {
+    unsigned long long cnt = min(shift, used - base);
+    for (unsigned long long i = threadIdx.x; i < cnt; i += BT)
+      sbase[base + i] = __ldcg(sbase + b0 + base + i);
+    __syncthreads();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    top = used;
+    bot = 0;
+  }
+  __syncthreads();
+}
+
 __global__ void __launch_bounds__(BT, 6)
 search_kernel(SearchParams P) {
   extern __shared__ uint32_t dyn[];
@@ -1191,6 +1236,7 @@ search_kernel(SearchParams P) {
         child_shape(sh, (uint32_t)code, s2, c2);
         if (!child_alive(sh, s2, c2)) continue;
         uint32_t len = 2 * s2 + 5;
+        stack_make_room(P, sbase, len, s_top, s_bot);
         if (t == 0) {
           bool tp;
           unsigned long long poff = 0;
@@ -1280,6 +1326,7 @@ search_kernel(SearchParams P) {
       if (sh.have) {
         // save the in-place task to the own stack (it is already counted)
         uint32_t len = 2 * sh.s + 5;
+        stack_make_room(P, sbase, len, s_top, s_bot);
         if (t == 0) {
           bool tp;
           unsigned long long poff = 0;

@@ -50,7 +50,7 @@ struct SlotHost {
 };
 
 struct Done {
-  scs_result r;
+  scs_result r{};
   std::vector<uint32_t> H;
 };
 
@@ -210,29 +210,29 @@ static int engine_init(scs_engine *E) {
   RC(E->dalloc(&sc.list, (size_t)E->grid * sc.stride, false));
   RC(E->dalloc(&sc.aux, (size_t)E->grid * sc.stride));
   RC(E->dalloc(&sc.tmp, (size_t)E->grid * 2 * sc.stride, false));
-  RC(E->dalloc(&sc.dsc, (size_t)E->grid * sc.stride, false));
-  // stacks
+  RC(E->dalloc(&sc.dsc, (size_t)E->grid * 3 * sc.stride));  // zeroed: scores
+  // stacks and pool: the task store is the engine's main memory consumer;
+  // stacks get most of what is free (DFS records of the largest local graph),
+  // the shared pool a quarter of the rest
   size_t free_b = 0, total_b = 0;
   CK(cudaMemGetInfo(&free_b, &total_b));
   uint64_t sw = c.stack_words;
+  uint64_t pw = c.pool_words;
+  uint64_t avail_words = (uint64_t)(free_b * 0.85) / 4;
+  if (!pw) pw = std::min<uint64_t>(avail_words / 4, 1ull << 33);
   if (!sw) {
-    // a few hundred root-sized records per CTA, capped by 40% of free memory
-    uint64_t want = std::max<uint64_t>(1ull << 20, (uint64_t)(2 * n + 5) * 64);
-    uint64_t cap = (uint64_t)(free_b * 0.4) / 4 / E->grid;
+    uint64_t want = std::max<uint64_t>(1ull << 20, (uint64_t)(2 * n + 5) * 4096);
+    uint64_t cap = (avail_words - std::min(pw, avail_words)) / E->grid;
     sw = std::min(want, cap);
   }
   E->stk.words = sw;
   RC(E->dalloc(&E->stk.base, (size_t)E->grid * sw, false));
   RC(E->dalloc(&E->stk.top, E->grid));
   RC(E->dalloc(&E->stk.bot, E->grid));
-  // pool
-  CK(cudaMemGetInfo(&free_b, &total_b));
-  uint64_t pw = c.pool_words;
-  if (!pw) pw = std::min<uint64_t>((uint64_t)(free_b * 0.5) / 4, 1ull << 31);
   E->pool.arena_cap = pw;
   RC(E->dalloc(&E->pool.arena, pw, false));
   RC(E->dalloc(&E->pool.arena_top, 1));
-  E->pool.desc_cap = 1u << 22;
+  E->pool.desc_cap = 1u << 24;
   RC(E->dalloc(&E->pool.desc, E->pool.desc_cap));
   RC(E->dalloc(&E->pool.head, 1));
   RC(E->dalloc(&E->pool.tail, 1));
