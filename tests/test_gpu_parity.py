@@ -166,31 +166,36 @@ def test_search_vs_bruteforce():
     eng.close()
 
 
+def _golden_c1():
+    return json.load(open(os.path.join(GOLD, "answers_chunglu_n4000.json")))
+
+
 def test_search_chunglu_golden(eng_c1, og_c1):
-    """All 50 queries of the 4000-vertex Chung-Lu workload against the
-    oracle's exact answers."""
+    """The config-1 queries the oracle solves within its node limit (33 of
+    50; the rest need tens of millions of tasks) against its exact answers;
+    every returned community is verified."""
     from oracle import verify_community
-    gold = json.load(open(os.path.join(GOLD, "answers_chunglu_n4000.json")))
-    rows = [(g["l"], g["h"], g["q"], g["heur"], g["limit_doms"]) for g in gold["queries"]]
+    gold = [g for g in _golden_c1()["queries"] if g["finished"]]
+    assert len(gold) >= 30
+    rows = [(g["l"], g["h"], g["q"], g["heur"], g["limit_doms"]) for g in gold]
     res = eng_c1.solve(rows)
-    checked = 0
-    for g, r in zip(gold["queries"], res):
+    for g, r in zip(gold, res):
         assert r["status"] in (0, 1), r
         assert r["kl_heuristic"] == g["kl_heu"]
-        if g["finished"]:
-            assert r["degree"] == g["degree"], (g, r)
-            checked += 1
+        assert r["degree"] == g["degree"], (g, r)
         c, hq, sz, md = verify_community(og_c1, r["H"], g["q"], g["l"], g["h"])
         if r["h_verified"]:
             assert c and hq and sz and md == r["degree"]
-    assert checked >= 40
+        if r["status"] == 0 and r["degree"] > g["kl_heu"]:
+            assert r["h_verified"] == 1, r
 
 
-def test_results_same_alone_and_in_mix(eng_c1, og_c1):
+def test_results_same_alone_and_in_mix(eng_c1):
     """A query's answer does not depend on what else runs with it."""
-    rows = [tuple(int(x) for x in r) for r in _queries_c1(og_c1)[:12]]
+    gold = [g for g in _golden_c1()["queries"] if g["finished"]][:12]
+    rows = [(g["l"], g["h"], g["q"], g["heur"], g["limit_doms"]) for g in gold]
     mix = eng_c1.solve(rows)
-    for row, m in zip(rows[:4], mix[:4]):
+    for row, m in zip(rows[:5], mix[:5]):
         alone = eng_c1.solve([row])[0]
         assert alone["degree"] == m["degree"]
         assert alone["status"] == m["status"]
