@@ -1,0 +1,321 @@
+"""Benchmark: exact size-bounded community search queries/sec on one GB300.
+
+Workload (one per GPU): the mid-size plain-GPU workload -- R-MAT scale 15
+(n = 32,768), exactly 16 * 2^15 unique undirected edges, (a, b, c) =
+(.57, .19, .19), graph seed 1234; 1,000 queries (seed 42): q uniform over
+vertices with core >= 8, l ~ U[3, 10], h = l + U[5, 30], heuristic on,
+dominating limit 10.  Warm-up steps use extra queries from seed 43.
+
+A step is one batch of `--batch` queries (default 100) submitted at once and
+run to completion; the timed steps cover the 1,000 queries once.  Every query
+carries the same search budget (`--node-budget` tasks, the stand-in for the
+reference's level cap, main.cu:444-463); a query that hits it reports the
+best degree found with status "timeout" (the reference's Overtime=1) and
+does not count as exact.
+
+value  = queries / device time of the timed steps (CUDA events, graph
+         resident, queries already submitted);
+e2e    = queries / time of the same steps through the C ABI from host
+         buffers (submit, run, poll of results and communities).
+--impl reference times the reference's CPU path (the oracle port of its
+branch-and-bound on the reference's heuristics) on the host cores.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "exact queries/sec + p50/p99 latency"
+UNIT = "queries/s"
+WORKLOAD = "rmat_s15_ef16_q1000"
+
+
+def env_rank():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+def build_workload(batch, warmup, steps):
+    from scs_gb300 import workloads as W
+    n, u, v = W.rmat(15, 16 << 15)
+    off, adj = W.to_csr(n, u, v)
+    return n, off, adj
+
+
+def queries_for(core, count, seed):
+    from scs_gb300 import workloads as W
+    return W.queries_mid(core, count=count, seed=seed)
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    def __init__(self, path):
+        self.path = path
+        self.proc = None
+
+    def start(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,"
+                 "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self, gpu_index=0):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sms, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9 or p[0] != str(gpu_index):
+                continue
+            try:
+                sms.append(float(p[1]))
+                mx = float(p[2])
+            except ValueError:
+                continue
+            for nm, val in zip(names, p[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        if not sms:
+            return None
+        return {"sm_mhz": float(np.median(sms)), "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sms)}
+
+
+def flush_l2(torch, buf):
+    # write a buffer larger than L2 (129 MB) between timed steps
+    buf.fill_(1.0)
+
+
+def measured_peak_gbs():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        try:
+            return float(json.load(open(p))["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+def cpu_baseline(n, off, adj, rows, budget, cap_s=10.0, procs=None):
+    """The CPU port (the reference's heuristics + its branch-and-bound rules,
+    oracle.c) on the host cores: one sampled query per process, same node
+    budget as the GPU plus a wall-clock cap per query.  Returns (qps, cores,
+    description).  Throughput = cores / mean per-query time; a capped query
+    counts with its capped time, which can only favour the CPU."""
+    import multiprocessing as mp
+    procs = procs or min(16, os.cpu_count() or 1)
+    rows = rows[:procs]
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(len(rows), initializer=_cpu_init, initargs=(n, off, adj, cap_s)) as pool:
+        out = pool.map(_cpu_solve, [(tuple(int(x) for x in r), budget) for r in rows])
+    times = [o[0] for o in out]
+    capped = sum(1 for o in out if o[2] == 2)
+    qps = len(rows) / max(np.mean(times), 1e-9) if times else 0.0
+    desc = ("%d queries, one per core, node budget %d, cap %.0f s per query; "
+            "%d hit the cap, %d the node budget; mean %.2f s per query, %.0f tasks/s/core"
+            % (len(rows), budget, cap_s, capped, sum(1 for o in out if o[2] == 1),
+               float(np.mean(times)), sum(o[1] for o in out) / max(sum(times), 1e-9)))
+    return qps, len(rows), desc
+
+
+_CPU_G = None
+
+
+def _cpu_init(n, off, adj, cap_s):
+    global _CPU_G
+    import oracle as O
+    _CPU_G = O.OracleGraph(n, off, adj)
+    O.lib().orc_set_time_limit(cap_s)
+
+
+def _cpu_solve(args):
+    row, budget = args
+    l, h, q, hf, ld = row
+    t0 = time.perf_counter()
+    r, _ = _CPU_G.solve(l, h, q, hf, ld, node_limit=budget)
+    return time.perf_counter() - t0, int(r.nodes), int(r.status)
+
+
+def run_reference(args):
+    rank, world, _ = env_rank()
+    if rank != 0:
+        return 0
+    n, off, adj = build_workload(args.batch, args.warmup, args.steps)
+    import oracle as O
+    og = O.OracleGraph(n, off, adj)
+    rows = queries_for(og.core, 1000, 42)
+    warm = queries_for(og.core, args.batch * args.warmup, 43)
+    procs = min(16, os.cpu_count() or 1)
+    for i in range(args.warmup):
+        cpu_baseline(n, off, adj, warm[i * args.batch:(i + 1) * args.batch], args.node_budget,
+                     cap_s=args.cpu_cap, procs=procs)
+    vals, samples = [], []
+    for i in range(args.steps):
+        qps, cores, sample = cpu_baseline(n, off, adj, rows[i * args.batch:(i + 1) * args.batch],
+                                          args.node_budget, cap_s=args.cpu_cap, procs=procs)
+        vals.append(qps)
+        samples.append(sample)
+    v = float(np.mean(vals))
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * args.batch / v,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+            "data": "synthetic", "config": {"workload": WORKLOAD, "batch": args.batch,
+                                            "node_budget": args.node_budget},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": procs, "kind": "port",
+                             "sample": "per step (first of %d): " % len(samples) + samples[0]},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--batch", type=int, default=100)
+    ap.add_argument("--node-budget", type=int, default=100000)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-cap", type=float, default=10.0,
+                    help="wall-clock cap per query on the CPU arms (seconds)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    rank, world, local = env_rank()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    from scs_gb300.engine import Engine
+
+    n, off, adj = build_workload(args.batch, args.warmup, args.steps)
+    eng = Engine(csr=(n, off, adj), limit_queries=max(args.batch, 1), slice_us=20000,
+                 node_budget=args.node_budget, device=local)
+    core = eng.core_numbers()
+    # weak scaling: every rank runs the full 1,000-query workload of its own
+    # query seed (rank 0 uses the workload's seed 42)
+    rows = queries_for(core, 1000, 42 + 1000 * rank)
+    warm = queries_for(core, args.batch * args.warmup, 43 + 1000 * rank)
+    flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda")  # 256 MB > L2
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+
+    for i in range(args.warmup):
+        eng.solve([tuple(int(x) for x in r) for r in warm[i * args.batch:(i + 1) * args.batch]])
+    st0 = eng.stats()
+    clocks = Clocks(os.path.join(ROOT, "gpurun_out", "clocks_r%d.csv" % rank)
+                    if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "/tmp/scs_clocks_%d.csv" % rank)
+    results, dev_ms, wall = [], 0.0, 0.0
+    h2d = d2h = 0
+    barrier()
+    clocks.start()
+    for i in range(args.steps):
+        batch = [tuple(int(x) for x in r) for r in rows[i * args.batch:(i + 1) * args.batch]]
+        flush_l2(torch, flush)
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0 = time.perf_counter()
+        e0.record()
+        res = eng.solve(batch)  # submit from host buffers, run, poll results
+        e1.record()
+        torch.cuda.synchronize()
+        wall += time.perf_counter() - t0
+        dev_ms += e0.elapsed_time(e1)
+        results += res
+    barrier()
+    ck = clocks.stop(local)
+    st1 = eng.stats()
+    # max over ranks
+    total_q = len(results)
+    t_dev = dev_ms / 1e3
+    if dist is not None:
+        t = torch.tensor([t_dev, wall], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_dev, wall = float(t[0]), float(t[1])
+        q = torch.tensor([total_q], dtype=torch.float64, device="cuda")
+        dist.all_reduce(q)
+        total_q = int(q[0])
+    lat = np.array([r["latency_ns"] for r in results]) / 1e6
+    exact = sum(1 for r in results if r["status"] in (0, 1))
+    verified = sum(1 for r in results if r["h_verified"])
+    search_ns = st1["search_ns"] - st0["search_ns"]
+    nbytes = st1["bytes"] - st0["bytes"]
+    launches = st1["launches"] - st0["launches"]
+    slices = st1["slices"] - st0["slices"]
+    peak, peak_kind = measured_peak_gbs()
+    achieved = (nbytes / (search_ns / 1e9) / 1e9) if search_ns else 0.0
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "search_traffic.json")
+    if os.path.exists(tp):
+        try:
+            traffic = json.load(open(tp)).get("dram_bytes_per_launch")
+        except Exception:
+            traffic = None
+    line = {
+        "metric": METRIC, "value": total_q / t_dev, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * t_dev / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "graph": "R-MAT scale 15, 524288 edges",
+                   "queries": total_q, "batch": args.batch, "node_budget": args.node_budget,
+                   "l2": "flushed between steps (256 MB write)",
+                   "exact_fraction": exact / max(len(results), 1),
+                   "verified_fraction": verified / max(len(results), 1),
+                   "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                   "nodes": st1["nodes"] - st0["nodes"], "parallelism": "replicas" if world > 1 else "1 GPU"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak if peak else None, "traffic": traffic,
+                     "peak_kind": peak_kind, "kernel": "search_kernel",
+                     "launches": slices},
+        "e2e": {"value": total_q / wall, "unit": UNIT,
+                "h2d_bytes_per_step": (st1["h2d_bytes"] - st0["h2d_bytes"]) // max(args.steps, 1)
+                + 20 * args.batch,
+                "d2h_bytes_per_step": (st1["d2h_bytes"] - st0["d2h_bytes"]) // max(args.steps, 1)},
+        "gpu_launches": launches,
+        "clocks": ck,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        sample = rows[: min(64, len(rows))]
+        qps, cores, desc = cpu_baseline(n, off, adj, sample, args.node_budget, args.cpu_cap)
+        line["cpu_baseline"] = {"value": qps, "unit": UNIT, "cores": cores, "kind": "port",
+                                "sample": desc}
+    eng.close()
+    if rank == 0:
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -137,7 +137,9 @@ enum {
   SCS_STAT_PREP_BYTES = 6,/* algorithmic bytes moved by preprocessing */
   SCS_STAT_SEARCH_NS = 7, /* device time inside search slices */
   SCS_STAT_PREP_NS = 8,   /* device time inside preprocessing */
-  SCS_STAT_LAUNCHES = 9   /* kernel launches issued */
+  SCS_STAT_LAUNCHES = 9,  /* kernel launches issued */
+  SCS_STAT_H2D = 10,      /* host-to-device bytes copied by the engine */
+  SCS_STAT_D2H = 11       /* device-to-host bytes copied by the engine */
 };
 int scs_stats(scs_engine *e, uint64_t *out);
 

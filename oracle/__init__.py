@@ -68,6 +68,7 @@ def lib():
         L.orc_solve.argtypes = [C.POINTER(Graph), C.c_uint32, C.c_uint32,
                                 C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
                                 C.c_uint64, C.POINTER(Result), _u32p, C.c_uint32]
+        L.orc_set_time_limit.argtypes = [C.c_double]
         L.orc_bruteforce.argtypes = [C.POINTER(Graph), C.c_uint32, C.c_uint32,
                                      C.c_uint32, C.c_uint32]
         L.orc_bruteforce.restype = C.c_uint32

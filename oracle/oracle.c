@@ -2,9 +2,11 @@
  * oracle.c -- CPU restatement of the SCS hot path (test infrastructure only;
  * see oracle.h).  Every function names the reference code it restates.
  */
+#define _POSIX_C_SOURCE 199309L
 #include "oracle.h"
 
 #include <ctype.h>
+#include <time.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -840,6 +842,14 @@ done:
 /* ------------------------------------------------------------------ */
 typedef struct { uint32_t *e; uint32_t s; } stk_ent;
 
+static double g_time_limit = 0.0; /* seconds per solve, 0 = none */
+void orc_set_time_limit(double seconds) { g_time_limit = seconds; }
+static double now_s(void) {
+  struct timespec ts;
+  clock_gettime(CLOCK_MONOTONIC, &ts);
+  return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+
 int orc_solve(const orc_graph *g, uint32_t l, uint32_t h, uint32_t q,
               uint32_t heur, uint32_t limit_doms, uint32_t rules,
               uint64_t node_limit, orc_result *res, uint32_t *H,
@@ -897,8 +907,11 @@ int orc_solve_from(const orc_graph *g, uint32_t l, uint32_t h, uint32_t q,
   uint32_t *doms = (uint32_t *)malloc((limit_doms + 1) * sizeof(uint32_t));
   uint64_t kcap = 0;
   uint32_t *kids = NULL;
+  const double t_start = now_s();
   while (sn) {
     if (node_limit && res->nodes >= node_limit) { res->status = 1; break; }
+    if (g_time_limit > 0 && (res->nodes & 15) == 0 &&
+        now_s() - t_start > g_time_limit) { res->status = 2; break; }
     stk_ent t = stk[--sn];
     res->nodes++;
     res->sum_task += t.s;

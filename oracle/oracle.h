@@ -46,7 +46,7 @@ typedef struct {
   uint32_t ubd;     /* distance bound used by the initial filter */
   uint32_t n_kept;  /* vertices passing core>kl && dist<=ubD */
   uint32_t n_local; /* of those, the ones in q's component */
-  uint32_t status;  /* 0 ok, 1 node limit reached */
+  uint32_t status;  /* 0 ok, 1 node limit reached, 2 time limit reached */
   uint64_t nodes;   /* tasks processed */
   uint64_t max_task;
   uint64_t sum_task;
@@ -81,6 +81,9 @@ uint32_t orc_cssc_heu(const orc_graph *g, uint32_t l, uint32_t h, uint32_t q,
                       uint32_t *H, uint32_t *hsize);
 
 /* ---- full query ---- */
+/* Wall-clock cap per orc_solve call (seconds, 0 = none; per process). */
+void orc_set_time_limit(double seconds);
+
 int orc_solve(const orc_graph *g, uint32_t l, uint32_t h, uint32_t q,
               uint32_t heur, uint32_t limit_doms, uint32_t rules,
               uint64_t node_limit, orc_result *res, uint32_t *H,

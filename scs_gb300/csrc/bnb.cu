@@ -39,6 +39,7 @@ struct Sh {
   uint32_t doms_idx[MAX_DOMS];
   uint32_t wit_pending;
   uint32_t bt;
+  unsigned long long bytes;  // algorithmic bytes accumulated by this CTA
   int have;
   int stop;
   unsigned long long rec;
@@ -311,6 +312,18 @@ __device__ void rule3(Task &T, Sh &sh) {
 __device__ void rule12(Task &T, Sh &sh, bool test) {
   const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
   const uint32_t h = sh.h, rules = sh.rules;
+  {
+    // algorithmic bytes of this visit: 16 B per entry (vertex, status, dR,
+    // dC) plus one pass over the entries' local adjacency
+    uint32_t dsum = 0;
+    for (uint32_t i = t; i < sh.s; i += BT) {
+      uint32_t x = T.list[i];
+      dsum += T.off[x + 1] - T.off[x];
+    }
+    dsum = warp_sum(dsum);
+    if (lane == 0) atomicAdd(&sh.bytes, 4ull * dsum);
+    if (t == 0) atomicAdd(&sh.bytes, 16ull * sh.s);
+  }
   if (rules & (R_RED1 | R_RED2)) {
     for (;;) {
       refresh_kl(T, sh, test);
@@ -954,7 +967,10 @@ step_test_kernel(SearchParams P) {
   if (ti >= P.t_ntasks) return;
   const uint32_t *rec = P.t_rec + P.t_rec_off[ti];
   set_task_header(P, sh, rec);
-  if (threadIdx.x == 0) sh.kl = P.t_kl[ti];
+  if (threadIdx.x == 0) {
+    sh.kl = P.t_kl[ti];
+    sh.bytes = 0;
+  }
   __syncthreads();
   Task T = make_task(P, sh, dyn, ti);
   for (uint32_t i = threadIdx.x; i < sh.n_local && T.W == dyn; i += BT) dyn[i] = 0;
@@ -1147,6 +1163,7 @@ search_kernel(SearchParams P) {
     s_hungry = 0;
     sh.have = 0;
     sh.stop = 0;
+    sh.bytes = 0;
   }
   __syncthreads();
   Task T;
@@ -1264,13 +1281,17 @@ search_kernel(SearchParams P) {
           write_child(T, sh, (uint32_t)code, r + REC_HDR, r + REC_HDR + s2, r);
         }
         __syncthreads();
-        if (t == 0 && s_pool_rec) publish_pool(P, s_pool_off);
+        if (t == 0) {
+          if (s_pool_rec) publish_pool(P, s_pool_off);
+          sh.bytes += 16ull * s2;
+        }
         pushed++;
       }
       uint32_t s2, c2;
       child_shape(sh, 0, s2, c2);
       cont = child_alive(sh, s2, c2);
       if (cont) {
+        if (t == 0) sh.bytes += 16ull * s2;
         apply_include(T, sh);
         pushed++;
       } else {
@@ -1373,6 +1394,7 @@ search_kernel(SearchParams P) {
     P.stk.top[cta] = s_top;
     P.stk.bot[cta] = s_bot;
     atomicAdd(&P.ctr->nodes, local_nodes);
+    atomicAdd(&P.ctr->bytes, sh.bytes);
   }
 }
 

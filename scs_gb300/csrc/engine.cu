@@ -65,7 +65,8 @@ struct scs_engine {
   int dev = 0;
   int num_sms = 0;
   cudaStream_t stream = nullptr;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
+  bool prep_pending = false;
 
   // device graph
   uint32_t *d_off = nullptr, *d_adj = nullptr, *d_core = nullptr;
@@ -138,6 +139,8 @@ static int engine_init(scs_engine *E) {
   CK(cudaStreamCreateWithFlags(&E->stream, cudaStreamNonBlocking));
   CK(cudaEventCreate(&E->ev0));
   CK(cudaEventCreate(&E->ev1));
+  CK(cudaEventCreate(&E->ev2));
+  CK(cudaEventCreate(&E->ev3));
   E->rules = c.rules_set ? ((c.red1 ? R_RED1 : 0) | (c.red2 ? R_RED2 : 0) |
                             (c.red3 ? R_RED3 : 0) | (c.prun1 ? R_PRUN1 : 0) |
                             (c.prun2 ? R_PRUN2 : 0))
@@ -386,9 +389,13 @@ static int admit(scs_engine *E) {
   if (jobs.empty()) return 0;
   cudaMemcpyAsync(E->d_jobs, jobs.data(), jobs.size() * sizeof(PrepJob),
                   cudaMemcpyHostToDevice, E->stream);
+  E->stats[SCS_STAT_H2D] += jobs.size() * sizeof(PrepJob);
+  cudaEventRecord(E->ev2, E->stream);
   prep_kernel<<<(unsigned)jobs.size(), PREP_THREADS, 0, E->stream>>>(
       DevGraph{n, E->g.dmax, E->d_off, E->d_adj, E->d_core}, E->sa, E->d_slots,
       E->d_jobs, (int)jobs.size(), E->ps, E->pool, E->d_ctr);
+  cudaEventRecord(E->ev3, E->stream);
+  E->prep_pending = true;
   E->stats[SCS_STAT_LAUNCHES]++;
   E->running += (uint32_t)jobs.size();
   return (int)jobs.size();
@@ -424,6 +431,15 @@ static int slice(scs_engine *E) {
   float ms = 0;
   cudaEventElapsedTime(&ms, E->ev0, E->ev1);
   E->stats[SCS_STAT_SEARCH_NS] += (uint64_t)(ms * 1e6);
+  if (E->prep_pending) {
+    float pm = 0;
+    cudaEventElapsedTime(&pm, E->ev2, E->ev3);
+    E->stats[SCS_STAT_PREP_NS] += (uint64_t)(pm * 1e6);
+    E->prep_pending = false;
+  }
+  E->stats[SCS_STAT_BYTES] = hc.bytes;
+  E->stats[SCS_STAT_D2H] += E->nslots * sizeof(Slot) + sizeof(Counters) + 8;
+  E->stats[SCS_STAT_H2D] += 24;
   E->stats[SCS_STAT_NODES] = hc.nodes;
   E->stats[SCS_STAT_DONATIONS] = hc.donations;
   E->stats[SCS_STAT_STEALS] = hc.steals;
@@ -449,6 +465,7 @@ static int slice(scs_engine *E) {
       H.resize(s.wit_n);
       CK(cudaMemcpy(H.data(), E->sa.witness + (size_t)i * E->sa.wit_cap,
                     s.wit_n * 4ull, cudaMemcpyDeviceToHost));
+      E->stats[SCS_STAT_D2H] += s.wit_n * 4ull;
     } else {
       H = sh.heuH;
     }
@@ -457,6 +474,7 @@ static int slice(scs_engine *E) {
     finish_result(E, i, degree, st, s.nodes, sns, H);
     Slot clear{};
     CK(cudaMemcpyAsync(E->d_slots + i, &clear, sizeof(Slot), cudaMemcpyHostToDevice, E->stream));
+    E->stats[SCS_STAT_H2D] += sizeof(Slot);
     E->running--;
   }
   // pool reset when fully drained
@@ -590,6 +608,8 @@ int scs_destroy(scs_engine *E) {
   for (void *p : E->allocs) cudaFree(p);
   if (E->ev0) cudaEventDestroy(E->ev0);
   if (E->ev1) cudaEventDestroy(E->ev1);
+  if (E->ev2) cudaEventDestroy(E->ev2);
+  if (E->ev3) cudaEventDestroy(E->ev3);
   if (E->stream) cudaStreamDestroy(E->stream);
   delete E;
   return 0;

@@ -22,7 +22,8 @@ STATUS_NAMES = {DONE: "done", HEURISTIC: "heuristic", CAPACITY: "capacity",
                 TIMEOUT: "timeout", BAD_QUERY: "bad_query", TOO_LARGE: "too_large"}
 
 STAT_NAMES = ["nodes", "slices", "donations", "steals", "spills", "bytes",
-              "prep_bytes", "search_ns", "prep_ns", "launches"]
+              "prep_bytes", "search_ns", "prep_ns", "launches", "h2d_bytes",
+              "d2h_bytes"]
 
 
 class Config(C.Structure):
