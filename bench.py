@@ -276,9 +276,10 @@ def main():
     achieved = (nbytes / (search_ns / 1e9) / 1e9) if search_ns else 0.0
     traffic = None
     tp = os.path.join(ROOT, "profiles", "search_traffic.json")
-    if os.path.exists(tp):
+    if os.path.exists(tp) and slices:
         try:
-            traffic = json.load(open(tp)).get("dram_bytes_per_launch")
+            rate = float(json.load(open(tp))["dram_bytes_per_ms"])
+            traffic = rate * (search_ns / 1e6) / slices  # DRAM bytes per launch
         except Exception:
             traffic = None
     line = {
@@ -296,7 +297,9 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak if peak else None, "traffic": traffic,
                      "peak_kind": peak_kind, "kernel": "search_kernel",
-                     "launches": slices},
+                     "launches": slices,
+                     "algorithmic_bytes_per_launch": nbytes / max(slices, 1),
+                     "mean_launch_ms": search_ns / 1e6 / max(slices, 1)},
         "e2e": {"value": total_q / wall, "unit": UNIT,
                 "h2d_bytes_per_step": (st1["h2d_bytes"] - st0["h2d_bytes"]) // max(args.steps, 1)
                 + 20 * args.batch,
