@@ -202,6 +202,9 @@ def main():
     ap.add_argument("--cpu-cap", type=float, default=10.0,
                     help="wall-clock cap per query on the CPU arms (seconds)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ctas-per-sm", type=int, default=0,
+                    help="search CTAs per SM (0: autotuned on the warm-up queries)")
+    ap.add_argument("--slice-us", type=int, default=0)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -216,13 +219,21 @@ def main():
     from scs_gb300.engine import Engine
 
     n, off, adj = build_workload(args.batch, args.warmup, args.steps)
-    eng = Engine(csr=(n, off, adj), limit_queries=max(args.batch, 1), slice_us=20000,
+    from scs_gb300.engine import core_numbers
+    core = core_numbers(n, off, adj)
+    warm = queries_for(core, args.batch * args.warmup, 43 + 1000 * rank)
+    tune = {"ctas_per_sm": args.ctas_per_sm, "slice_us": args.slice_us or 20000}
+    if not args.ctas_per_sm:
+        # launch shape chosen by the autotuner on warm-up queries (not timed)
+        from scs_gb300.autotune import autotune
+        sample = [tuple(int(x) for x in r) for r in warm[: min(len(warm), 64)]]
+        tune, _ = autotune(n, off, adj, sample, args.node_budget, device=local)
+    eng = Engine(csr=(n, off, adj), limit_queries=max(args.batch, 1),
+                 slice_us=tune["slice_us"], ctas_per_sm=tune["ctas_per_sm"],
                  node_budget=args.node_budget, device=local)
-    core = eng.core_numbers()
     # weak scaling: every rank runs the full 1,000-query workload of its own
     # query seed (rank 0 uses the workload's seed 42)
     rows = queries_for(core, 1000, 42 + 1000 * rank)
-    warm = queries_for(core, args.batch * args.warmup, 43 + 1000 * rank)
     flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda")  # 256 MB > L2
 
     def barrier():
@@ -293,7 +304,8 @@ def main():
                    "exact_fraction": exact / max(len(results), 1),
                    "verified_fraction": verified / max(len(results), 1),
                    "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-                   "nodes": st1["nodes"] - st0["nodes"], "parallelism": "replicas" if world > 1 else "1 GPU"},
+                   "nodes": st1["nodes"] - st0["nodes"], "parallelism": "replicas" if world > 1 else "1 GPU",
+                   "ctas_per_sm": tune["ctas_per_sm"], "slice_us": tune["slice_us"]},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak if peak else None, "traffic": traffic,
                      "peak_kind": peak_kind, "kernel": "search_kernel",

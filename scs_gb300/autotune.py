@@ -1,0 +1,70 @@
+"""Autotuner: picks the search launch shape per graph and query-size range.
+
+Swept parameters (the engine's counterparts of the reference's compile-time
+BLK_NUMS/BLK_DIM and its partition/limitTasks arguments, inc/Intialize.h:26-31,
+main.cu:484-497):
+
+* ``ctas_per_sm`` -- search CTAs per SM; it also sets how many per-vertex
+  state words fit in shared memory (the shared-memory staging threshold:
+  local graphs above it keep their state in L2-resident global memory);
+* ``slice_us``    -- length of one persistent search launch.
+
+Each candidate runs the same sample of queries under the same node budget;
+the fastest wins.  Results are cached as JSON keyed by a checksum of the
+graph and the sample's h range.
+"""
+import hashlib
+import json
+import os
+import time
+
+import numpy as np
+
+CACHE_DIR = os.environ.get("SCS_TUNE_DIR", os.path.join(os.path.expanduser("~"), ".cache", "scs_gb300"))
+DEFAULT_GRID = [(6, 20000), (4, 20000), (3, 20000), (2, 20000)]
+
+
+def graph_key(off, adj, rows):
+    h = hashlib.sha256()
+    h.update(np.asarray(off, dtype=np.uint32).tobytes())
+    h.update(np.asarray(adj, dtype=np.uint32).tobytes())
+    hs = [int(r[1]) for r in rows]
+    return "%s_h%d-%d" % (h.hexdigest()[:16], min(hs), max(hs))
+
+
+def autotune(n, off, adj, rows, node_budget, grid=DEFAULT_GRID, use_cache=True,
+             verbose=False, device=0):
+    """Return (best_config_dict, trials).  rows: list of query tuples."""
+    from .engine import Engine
+    key = graph_key(off, adj, rows)
+    path = os.path.join(CACHE_DIR, key + ".json")
+    if use_cache and os.path.exists(path):
+        try:
+            d = json.load(open(path))
+            return d["best"], d["trials"]
+        except Exception:
+            pass
+    trials = []
+    for cps, slice_us in grid:
+        eng = Engine(csr=(n, off, adj), limit_queries=len(rows), ctas_per_sm=cps,
+                     slice_us=slice_us, node_budget=node_budget, stack_words=1 << 22,
+                     pool_words=1 << 28, device=device)
+        t0 = time.perf_counter()
+        res = eng.solve(rows)
+        dt = time.perf_counter() - t0
+        st = eng.stats()
+        eng.close()
+        trial = {"ctas_per_sm": cps, "slice_us": slice_us, "seconds": dt,
+                 "qps": len(rows) / dt, "nodes": st["nodes"],
+                 "exact": sum(1 for r in res if r["status"] in (0, 1))}
+        trials.append(trial)
+        if verbose:
+            print("autotune", trial, flush=True)
+    best = max(trials, key=lambda t: t["qps"])
+    best = {"ctas_per_sm": best["ctas_per_sm"], "slice_us": best["slice_us"]}
+    try:
+        os.makedirs(CACHE_DIR, exist_ok=True)
+        json.dump({"best": best, "trials": trials}, open(path, "w"))
+    except OSError:
+        pass
+    return best, trials

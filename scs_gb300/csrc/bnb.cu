@@ -40,6 +40,7 @@ struct Sh {
   uint32_t wit_pending;
   uint32_t bt;
   unsigned long long bytes;  // algorithmic bytes accumulated by this CTA
+  float mean_deg;            // local CSR entries per local vertex (this query)
   int have;
   int stop;
   unsigned long long rec;
@@ -52,6 +53,7 @@ struct Sh {
   uint32_t hist[CL_CAP + 1];
   uint32_t kid_len[MAX_DOMS + 2];
   unsigned long long kid_dst[MAX_DOMS + 2];
+  unsigned long long kid_pool[MAX_DOMS + 2];
 };
 
 __device__ __forceinline__ uint32_t st_of(uint32_t w) { return w >> 30; }
@@ -312,17 +314,11 @@ __device__ void rule3(Task &T, Sh &sh) {
 __device__ void rule12(Task &T, Sh &sh, bool test) {
   const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
   const uint32_t h = sh.h, rules = sh.rules;
-  {
+  if (t == 0) {
     // algorithmic bytes of this visit: 16 B per entry (vertex, status, dR,
-    // dC) plus one pass over the entries' local adjacency
-    uint32_t dsum = 0;
-    for (uint32_t i = t; i < sh.s; i += BT) {
-      uint32_t x = T.list[i];
-      dsum += T.off[x + 1] - T.off[x];
-    }
-    dsum = warp_sum(dsum);
-    if (lane == 0) atomicAdd(&sh.bytes, 4ull * dsum);
-    if (t == 0) atomicAdd(&sh.bytes, 16ull * sh.s);
+    // dC) plus one pass over the entries' local adjacency, estimated with the
+    // query's mean local degree (local CSR entries / local vertices)
+    sh.bytes += 16ull * sh.s + (unsigned long long)(4.0f * sh.s * sh.mean_deg);
   }
   if (rules & (R_RED1 | R_RED2)) {
     for (;;) {
@@ -792,6 +788,43 @@ __device__ void write_child(Task &T, Sh &sh, uint32_t code, uint32_t *ent_dst,
   }
 }
 
+// Write every child code in [code_lo, code_hi] in one pass over the entries:
+// dst[code] is the record start (or null when the child is not written).
+__device__ void write_children(Task &T, Sh &sh, uint32_t code_lo,
+                               uint32_t code_hi, uint32_t *const *dst) {
+  const int t = threadIdx.x;
+  const uint32_t s = sh.s, k = sh.ndoms;
+  for (uint32_t i = t; i < s; i += BT) {
+    const uint32_t x = T.list[i];
+    const uint32_t a = T.aux[x];
+    const uint32_t w = T.W[x];
+    for (uint32_t code = code_lo; code <= code_hi; code++) {
+      uint32_t *d = dst[code];
+      if (!d || child_skip(a, code, k)) continue;
+      uint32_t s2, c2;
+      child_shape(sh, code, s2, c2);
+      uint32_t o = i - skipped_before(sh, i, code);
+      uint32_t ent, deg;
+      child_entry(x, w, a, code, k, ent, deg);
+      d[REC_HDR + o] = ent;
+      d[REC_HDR + s2 + o] = deg;
+    }
+  }
+  if (t == 0) {
+    for (uint32_t code = code_lo; code <= code_hi; code++) {
+      uint32_t *d = dst[code];
+      if (!d) continue;
+      uint32_t s2, c2;
+      child_shape(sh, code, s2, c2);
+      d[0] = sh.slot;
+      d[1] = s2;
+      d[2] = c2;
+      d[3] = 2 * s2 + 5;
+      d[REC_HDR + 2 * s2] = 2 * s2 + 5;
+    }
+  }
+}
+
 // apply the Include child to the in-CTA state (continue depth-first)
 __device__ void apply_include(Task &T, Sh &sh) {
   const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
@@ -951,6 +984,9 @@ __device__ void set_task_header(const SearchParams &P, Sh &sh,
     sh.kl = *(volatile uint32_t *)&sl->kl;
     sh.q_local = sl->q_local;
     sh.dmax = P.g.dmax;
+    sh.mean_deg = sl->n_local ? (float)P.sa.loc_off[(size_t)sh.slot * (P.sa.stride_n + 1) + sl->n_local] /
+                                    (float)sl->n_local
+                              : 0.0f;
   }
   __syncthreads();
 }
@@ -1254,14 +1290,27 @@ search_kernel(SearchParams P) {
     bool cont = false;
     if (sh.outcome == 0) {
       const uint32_t k = sh.ndoms;
-      // push Exclude, Dom_{k-1} .. Dom_0 (so Dom_0 pops first after the dive)
-      for (int code = (int)k + 1; code >= 1; code--) {
-        uint32_t s2, c2;
-        child_shape(sh, (uint32_t)code, s2, c2);
-        if (!child_alive(sh, s2, c2)) continue;
-        uint32_t len = 2 * s2 + 5;
-        stack_make_room(P, sbase, len, s_top, s_bot);
-        if (t == 0) {
+      // reserve Exclude, Dom_{k-1} .. Dom_0 in push order (Dom_0 on top, so
+      // it pops first after the dive), then write all of them in one pass.
+      // Room is made once for all of them: a compaction between two
+      // reservations would move the earlier ones.
+      {
+        unsigned long long total = 0;
+        for (uint32_t code = 1; code <= k + 1; code++) {
+          uint32_t s2, c2;
+          child_shape(sh, code, s2, c2);
+          if (child_alive(sh, s2, c2)) total += 2ull * s2 + 5;
+        }
+        if (total) stack_make_room(P, sbase, (uint32_t)min(total, 0xFFFFFFFFull), s_top, s_bot);
+      }
+      if (t == 0) {
+        for (int code = (int)k + 1; code >= 1; code--) {
+          uint32_t s2, c2;
+          child_shape(sh, (uint32_t)code, s2, c2);
+          sh.kid_dst[code] = 0;
+          sh.kid_len[code] = 0;
+          if (!child_alive(sh, s2, c2)) continue;
+          uint32_t len = 2 * s2 + 5;
           bool tp;
           unsigned long long poff = 0;
           unsigned long long top = s_top, bot = s_bot;
@@ -1269,30 +1318,30 @@ search_kernel(SearchParams P) {
           uint32_t *d = reserve_record(P, cta, len, top, bot, tp, poff);
           s_top = top;
           s_bot = bot;
-          s_rec = d;
-          s_pool_rec = tp ? 1 : 0;
-          s_pool_off = poff;
+          sh.kid_dst[code] = (unsigned long long)d;
+          sh.kid_len[code] = tp ? 0x80000000u : 1u;
+          sh.kid_pool[code] = poff;
           if (!d) {
             atomicOr(&P.ctr->error, ERR_STACK);
             P.slots[sh.slot].abort = 1;
             P.slots[sh.slot].status = RS_CAPACITY;
           }
         }
+      }
+      __syncthreads();
+      if (k + 1 >= 1) {
+        write_children(T, sh, 1, k + 1, (uint32_t *const *)sh.kid_dst);
         __syncthreads();
-        if (!s_rec) {
-          __syncthreads();
-          continue;
+        for (uint32_t code = 1; code <= k + 1; code++) {
+          if (!sh.kid_dst[code]) continue;
+          if (t == 0) {
+            uint32_t s2, c2;
+            child_shape(sh, code, s2, c2);
+            if (sh.kid_len[code] & 0x80000000u) publish_pool(P, sh.kid_pool[code]);
+            sh.bytes += 16ull * s2;
+          }
+          pushed++;
         }
-        {
-          uint32_t *r = s_rec;
-          write_child(T, sh, (uint32_t)code, r + REC_HDR, r + REC_HDR + s2, r);
-        }
-        __syncthreads();
-        if (t == 0) {
-          if (s_pool_rec) publish_pool(P, s_pool_off);
-          sh.bytes += 16ull * s2;
-        }
-        pushed++;
       }
       uint32_t s2, c2;
       child_shape(sh, 0, s2, c2);
