@@ -169,6 +169,33 @@ int scs_greedy_incumbent(uint32_t n, const uint32_t *off, const uint32_t *adj,
 /* Distance bound ubD from n(k, D) (main.cu:154-172). */
 uint32_t scs_distance_bound(uint32_t kl, uint32_t h);
 
+/* ---- allocation-free preprocessing (no counterpart in the reference) ----
+ * For callers that cannot call cudaMalloc -- code running inside another
+ * framework's memory pool or allocator hook, plugins whose host forbids
+ * device allocations after start-up, latency-critical loops that must not
+ * allocate.  Builds the filtered local graph of one query (bounded BFS from
+ * q, keep core > kl && dist <= ubd, q's component, local CSR) exactly like
+ * the engine's preprocessing, but allocates nothing: the caller passes the
+ * device graph (off[n+1], adj, core[n], max degree) and device outputs
+ * gid[n], dist[n], loc_off[n+1], loc_adj[loc_adj_cap] (rows ascending,
+ * padded to a multiple of 4 with 0xFFFFFFFF) and info[4] = {n_local,
+ * q_local, padded entries used, status: 0 ok, 1 loc_adj_cap too small}.
+ * Scratch is a fixed array inside the library for graphs of at most
+ * SCS_NOALLOC_MAX_N vertices (about 6 MB, held on every GPU that loads the
+ * library until exit); larger n is rejected with SCS_EINVAL.  The first call
+ * on a device looks up the array's device address, so make it before any
+ * stream capture.  All calls share the array: calls that overlap on the GPU
+ * race.  The kernel is enqueued on `stream` (a cudaStream_t, NULL for the
+ * default stream); results are ready when the stream is. */
+#define SCS_NOALLOC_MAX_N (1u << 19)
+int scs_local_graph_noalloc(const uint32_t *d_off, const uint32_t *d_adj,
+                            const uint32_t *d_core, uint32_t n, uint32_t dmax,
+                            uint32_t q, uint32_t kl, uint32_t ubd,
+                            uint32_t *d_gid, uint32_t *d_dist,
+                            uint32_t *d_loc_off, uint32_t *d_loc_adj,
+                            uint64_t loc_adj_cap, uint32_t *d_info,
+                            void *stream);
+
 /* ---- test hooks (used by the parity tests; no reference counterpart) ----
  * These expose single stages of the pipeline so they can be compared with
  * the CPU oracle.  They need an idle engine (no queries running). */

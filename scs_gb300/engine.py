@@ -89,6 +89,9 @@ def lib(build_if_missing=False):
                                        C.c_uint32, _u32p, _u32p, _u32p]
     L.scs_distance_bound.argtypes = [C.c_uint32, C.c_uint32]
     L.scs_distance_bound.restype = C.c_uint32
+    L.scs_local_graph_noalloc.argtypes = [vp, vp, vp, C.c_uint32, C.c_uint32, C.c_uint32,
+                                          C.c_uint32, C.c_uint32, vp, vp, vp, vp,
+                                          C.c_uint64, vp, vp]
     L.scs_debug_prepare.argtypes = [vp, C.c_uint32, C.POINTER(Query), _u32p, _u32p, _u32p, _u32p]
     L.scs_debug_local_graph.argtypes = [vp, C.c_uint32, _u32p, _u32p, _u32p, _u32p]
     L.scs_debug_step.argtypes = [vp, C.c_uint32, _u32p, _u32p, _u64p, _u32p, _u32p,
@@ -156,6 +159,20 @@ def greedy_incumbent(n, off, adj, l, h, q):
 
 def distance_bound(kl, h):
     return int(lib().scs_distance_bound(kl, h))
+
+
+NOALLOC_MAX_N = 1 << 19
+
+
+def local_graph_noalloc(d_off, d_adj, d_core, n, dmax, q, kl, ubd, d_gid, d_dist,
+                        d_loc_off, d_loc_adj, loc_adj_cap, d_info, stream=0):
+    """Allocation-free local-graph build (device pointers as ints); see
+    scs_local_graph_noalloc in include/scs.h."""
+    rc = lib().scs_local_graph_noalloc(d_off, d_adj, d_core, n, dmax, q, kl, ubd, d_gid,
+                                       d_dist, d_loc_off, d_loc_adj, loc_adj_cap, d_info,
+                                       stream)
+    if rc:
+        raise SCSError("scs_local_graph_noalloc failed (%d)" % rc)
 
 
 # ---------------------------------------------------------------------------
