@@ -169,6 +169,18 @@ int scs_greedy_incumbent(uint32_t n, const uint32_t *off, const uint32_t *adj,
 /* Distance bound ubD from n(k, D) (main.cu:154-172). */
 uint32_t scs_distance_bound(uint32_t kl, uint32_t h);
 
+/* ---- server surface (host only) ---- */
+
+/* Parse one queue message (main.cu:92-109): returns 0 and fills q for
+ * "<l> <h> <qid> <heuristic_flag> <limit_dominating_set>", 1 for
+ * "server_exit" (main.cu:51-60), SCS_EINVAL otherwise. */
+int scs_parse_message(const char *text, scs_query *q);
+
+/* Format a result as the reference's results-file row
+ * N1|N2|QID|Time|Degree|Overtime|Heu|TotalTime (main.cu:124-128, 328-333,
+ * 348-352, 451-454).  Returns the length or SCS_EINVAL. */
+int scs_format_result_row(const scs_result *r, char *buf, uint32_t cap);
+
 /* ---- allocation-free preprocessing (no counterpart in the reference) ----
  * For callers that cannot call cudaMalloc -- code running inside another
  * framework's memory pool or allocator hook, plugins whose host forbids

@@ -15,6 +15,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU = ["prep.cu", "bnb.cu", "engine.cu", "noalloc.cu"]
 CXX = ["host_graph.cpp", "host_api.cpp"]
 LIB = "libscs.so"
+EXES = {"scs_server": "server.cpp", "scs_client": "client.cpp"}
 
 
 def nvcc():
@@ -61,7 +62,16 @@ def build(verbose=False, force=False):
         list(ex.map(run, cmds))
     objs = [os.path.join(objdir, f + ".o") for f in CU + CXX]
     run([nvcc(), *ARCH, "-shared", "-o", out, *objs, "-lcudart", "-lpthread"])
+    # reference-compatible server and batch client, linked to the library
+    for exe, src in EXES.items():
+        run(["g++", "-O2", "-std=c++17", "-Wall", "-o", os.path.join(OUT, exe),
+             os.path.join(CSRC, src), "-L" + OUT, "-lscs", "-Wl,-rpath,$ORIGIN",
+             "-lpthread"])
     return out
+
+
+def exe_path(name):
+    return os.path.join(OUT, name)
 
 
 if __name__ == "__main__":

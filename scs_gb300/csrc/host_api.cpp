@@ -56,3 +56,89 @@ int scs_greedy_incumbent(uint32_t n, const uint32_t *off, const uint32_t *adj,
 uint32_t scs_distance_bound(uint32_t kl, uint32_t h) { return ubd_host(kl, h); }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// server surface helpers
+// ---------------------------------------------------------------------------
+#include <cctype>
+#include <sstream>
+
+#include "server_format.h"
+
+bool scs_is_server_exit(const std::string &str) {
+  std::string t = str;
+  size_t e = t.find_last_not_of(" \n\r\t");
+  if (e == std::string::npos) return false;
+  t.erase(e + 1);
+  t.erase(0, t.find_first_not_of(" \n\r\t"));
+  for (auto &c : t) c = (char)tolower((unsigned char)c);
+  return t == "server_exit";
+}
+
+bool scs_parse_query(const std::string &s, scs_query &q) {
+  std::istringstream iss(s);
+  std::vector<unsigned long long> v;
+  std::string tok;
+  while (iss >> tok) {
+    if (tok.empty() || tok.size() > 10) return false;
+    for (char c : tok)
+      if (!isdigit((unsigned char)c)) return false;
+    v.push_back(std::stoull(tok));
+  }
+  if (v.size() != 5) return false;
+  for (auto x : v)
+    if (x > 0xFFFFFFFFull) return false;
+  q.l = (uint32_t)v[0];
+  q.h = (uint32_t)v[1];
+  q.q = (uint32_t)v[2];
+  q.heuristic = (uint32_t)v[3];
+  q.limit_doms = (uint32_t)v[4];
+  return true;
+}
+
+std::string scs_group_thousands(long long number) {
+  std::vector<unsigned> seq;
+  if (number <= 0) seq.push_back(0);
+  while (number > 0) {
+    seq.push_back((unsigned)(number % 1000));
+    number /= 1000;
+  }
+  std::string res;
+  char buf[8];
+  for (size_t i = seq.size(); i > 0; i--) {
+    snprintf(buf, sizeof(buf), i == seq.size() ? "%u" : ",%03u", seq[i - 1]);
+    res += buf;
+  }
+  return res;
+}
+
+std::string scs_format_row(const scs_result &r) {
+  std::ostringstream os;
+  os << r.l << "|" << r.h << "|" << r.q << "|"
+     << scs_group_thousands((long long)(r.latency_ns / 1000)) << "|" << r.degree << "|";
+  switch (r.status) {
+    case SCS_HEURISTIC: os << "0|1|0"; break;  // main.cu:127
+    case SCS_TIMEOUT: os << "1|0"; break;      // main.cu:454 (7 fields)
+    case SCS_CAPACITY: os << "2|0|0"; break;   // main.cu:351
+    default: os << "0|0|0"; break;             // main.cu:332
+  }
+  return os.str();
+}
+
+extern "C" {
+
+int scs_parse_message(const char *text, scs_query *q) {
+  if (!text || !q) return SCS_EINVAL;
+  if (scs_is_server_exit(text)) return 1;
+  return scs_parse_query(text, *q) ? 0 : SCS_EINVAL;
+}
+
+int scs_format_result_row(const scs_result *r, char *buf, uint32_t cap) {
+  if (!r || !buf || !cap) return SCS_EINVAL;
+  std::string s = scs_format_row(*r);
+  if (s.size() + 1 > cap) return SCS_EINVAL;
+  memcpy(buf, s.c_str(), s.size() + 1);
+  return (int)s.size();
+}
+
+}  // extern "C"
