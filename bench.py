@@ -104,6 +104,18 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sms)}
 
 
+def reduce_over_ranks(dist, torch, t_dev, wall, queries, device):
+    """Replicas: whole-job time is the slowest rank's, throughput counts the
+    queries of every rank."""
+    if dist is None:
+        return t_dev, wall, queries
+    t = torch.tensor([t_dev, wall], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    q = torch.tensor([float(queries)], dtype=torch.float64, device=device)
+    dist.all_reduce(q)
+    return float(t[0]), float(t[1]), int(q[0])
+
+
 def flush_l2(torch, buf):
     # write a buffer larger than L2 (129 MB) between timed steps
     buf.fill_(1.0)
@@ -266,16 +278,9 @@ def main():
     barrier()
     ck = clocks.stop(local)
     st1 = eng.stats()
-    # max over ranks
-    total_q = len(results)
-    t_dev = dev_ms / 1e3
-    if dist is not None:
-        t = torch.tensor([t_dev, wall], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_dev, wall = float(t[0]), float(t[1])
-        q = torch.tensor([total_q], dtype=torch.float64, device="cuda")
-        dist.all_reduce(q)
-        total_q = int(q[0])
+    # max of the times over ranks, sum of the queries
+    t_dev, wall, total_q = reduce_over_ranks(dist, torch, dev_ms / 1e3, wall, len(results),
+                                             "cuda")
     lat = np.array([r["latency_ns"] for r in results]) / 1e6
     exact = sum(1 for r in results if r["status"] in (0, 1))
     verified = sum(1 for r in results if r["h_verified"])
