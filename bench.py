@@ -6,8 +6,10 @@ Workload (one per GPU): the mid-size plain-GPU workload -- R-MAT scale 15
 vertices with core >= 8, l ~ U[3, 10], h = l + U[5, 30], heuristic on,
 dominating limit 10.  Warm-up steps use extra queries from seed 43.
 
-A step is one batch of `--batch` queries (default 100) submitted at once and
-run to completion; the timed steps cover the 1,000 queries once.  Every query
+A step is one batch of `--batch` queries submitted at once and run to
+completion (default: the whole 1,000-query workload in one step, as the
+workload defines it, so the engine batches continuously across all of them);
+warm-up steps run `--warmup-batch` other queries each.  Every query
 carries the same search budget (`--node-budget` tasks, the stand-in for the
 reference's level cap, main.cu:444-463); a query that hits it reports the
 best degree found with status "timeout" (the reference's Overtime=1) and
@@ -178,12 +180,12 @@ def run_reference(args):
     n, off, adj = build_workload(args.batch, args.warmup, args.steps)
     import oracle as O
     og = O.OracleGraph(n, off, adj)
-    rows = queries_for(og.core, 1000, 42)
-    warm = queries_for(og.core, args.batch * args.warmup, 43)
+    rows = queries_for(og.core, args.batch * args.steps, 42)
+    warm = queries_for(og.core, args.warmup_batch * args.warmup, 43)
     procs = min(16, os.cpu_count() or 1)
     for i in range(args.warmup):
-        cpu_baseline(n, off, adj, warm[i * args.batch:(i + 1) * args.batch], args.node_budget,
-                     cap_s=args.cpu_cap, procs=procs)
+        cpu_baseline(n, off, adj, warm[i * args.warmup_batch:(i + 1) * args.warmup_batch],
+                     args.node_budget, cap_s=args.cpu_cap, procs=procs)
     vals, samples = [], []
     for i in range(args.steps):
         qps, cores, sample = cpu_baseline(n, off, adj, rows[i * args.batch:(i + 1) * args.batch],
@@ -206,9 +208,10 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=1)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--batch", type=int, default=100)
+    ap.add_argument("--batch", type=int, default=1000)
+    ap.add_argument("--warmup-batch", type=int, default=48)
     ap.add_argument("--node-budget", type=int, default=100000)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-cap", type=float, default=10.0,
@@ -233,7 +236,7 @@ def main():
     n, off, adj = build_workload(args.batch, args.warmup, args.steps)
     from scs_gb300.engine import core_numbers
     core = core_numbers(n, off, adj)
-    warm = queries_for(core, args.batch * args.warmup, 43 + 1000 * rank)
+    warm = queries_for(core, args.warmup_batch * args.warmup, 43 + 1000 * rank)
     tune = {"ctas_per_sm": args.ctas_per_sm, "slice_us": args.slice_us or 20000}
     if not args.ctas_per_sm:
         # launch shape chosen by the autotuner on warm-up queries (not timed)
@@ -245,7 +248,7 @@ def main():
                  node_budget=args.node_budget, device=local)
     # weak scaling: every rank runs the full 1,000-query workload of its own
     # query seed (rank 0 uses the workload's seed 42)
-    rows = queries_for(core, 1000, 42 + 1000 * rank)
+    rows = queries_for(core, args.batch * args.steps, 42 + 1000 * rank)
     flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda")  # 256 MB > L2
 
     def barrier():
@@ -253,8 +256,9 @@ def main():
         if dist is not None:
             dist.barrier()
 
+    wb = args.warmup_batch
     for i in range(args.warmup):
-        eng.solve([tuple(int(x) for x in r) for r in warm[i * args.batch:(i + 1) * args.batch]])
+        eng.solve([tuple(int(x) for x in r) for r in warm[i * wb:(i + 1) * wb]])
     st0 = eng.stats()
     clocks = Clocks(os.path.join(ROOT, "gpurun_out", "clocks_r%d.csv" % rank)
                     if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "/tmp/scs_clocks_%d.csv" % rank)
