@@ -143,6 +143,11 @@ enum {
 };
 int scs_stats(scs_engine *e, uint64_t *out);
 
+/* Search-kernel profile (16 u64): clock cycles spent per step phase summed
+ * over CTAs [0 load, 1 min degree + rule 3, 2 rules 1/2, 3 bounds, 4 ustar,
+ * 5 doms, 6 children, 7 other], then rule-1/2 rounds, rule-3 rounds, steps. */
+int scs_profile(scs_engine *e, uint64_t *out);
+
 /* Text of the last error on this engine (or the last creation failure). */
 const char *scs_last_error(scs_engine *e);
 

@@ -40,6 +40,9 @@ struct Sh {
   uint32_t wit_pending;
   uint32_t bt;
   unsigned long long bytes;  // algorithmic bytes accumulated by this CTA
+  unsigned long long ph[8];  // clock cycles per phase (thread 0)
+  unsigned long long t_ph;   // start of the current phase
+  unsigned long long r12, r3;
   float mean_deg;            // local CSR entries per local vertex (this query)
   int have;
   int stop;
@@ -146,6 +149,15 @@ __device__ __forceinline__ void warp_append(bool want, uint32_t val,
   if (lane == __ffs(m) - 1) base = atomicAdd(cnt, __popc(m));
   base = __shfl_sync(0xffffffffu, base, __ffs(m) - 1);
   if (want) dst[base + __popc(m & ((1u << lane) - 1u))] = val;
+}
+
+__device__ __forceinline__ void phase_mark(Sh &sh, int which) {
+  // thread 0 only: charge the cycles since the last mark to phase `which`
+  if (threadIdx.x == 0) {
+    unsigned long long now = clock64();
+    sh.ph[which] += now - sh.t_ph;
+    sh.t_ph = now;
+  }
 }
 
 struct Task {
@@ -284,6 +296,7 @@ __device__ void rule3(Task &T, Sh &sh) {
     }
     __syncthreads();
     const uint32_t np = sh.cnt[2];
+    if (t == 0) sh.r3++;
     if (np == 0) break;
     for (uint32_t i = t; i < np; i += BT) {
       uint32_t x = T.tmp[i];
@@ -347,6 +360,7 @@ __device__ void rule12(Task &T, Sh &sh, bool test) {
       }
       __syncthreads();
       const uint32_t nr = sh.cnt[1];
+      if (t == 0) sh.r12++;
       if (nr == 0) break;
       for (uint32_t i = t; i < nr; i += BT) T.W[T.tmp[i]] = ST_X << 30;
       __syncthreads();
@@ -899,6 +913,7 @@ __device__ void step_core(Task &T, Sh &sh, bool test, uint32_t *t_wit) {
     sh.nR = 0;
   }
   __syncthreads();
+  phase_mark(sh, 7);
   refresh_kl(T, sh, test);
   if (sh.csize > sh.h) {
     if (t == 0) sh.outcome = 1;
@@ -917,13 +932,16 @@ __device__ void step_core(Task &T, Sh &sh, bool test, uint32_t *t_wit) {
     }
     if (sh.csize != c0 && sh.l <= sh.csize) eval_mindeg(T, sh, test, t_wit);
   }
+  phase_mark(sh, 1);
   if (sh.csize >= sh.h) {
     if (t == 0) sh.outcome = 1;
     __syncthreads();
     return;
   }
   rule12(T, sh, test);
+  phase_mark(sh, 2);
   bounds(T, sh);
+  phase_mark(sh, 3);
   refresh_kl(T, sh, test);
   uint32_t ub = min(sh.p1, sh.p2);
   if (ub <= sh.kl) {
@@ -937,6 +955,7 @@ __device__ void step_core(Task &T, Sh &sh, bool test, uint32_t *t_wit) {
     return;
   }
   choose_ustar(T, sh);
+  phase_mark(sh, 4);
   if (sh.ustar == UINT32_MAX) {
     clear_scores(T, sh);
     if (t == 0) sh.outcome = 3;
@@ -946,6 +965,7 @@ __device__ void step_core(Task &T, Sh &sh, bool test, uint32_t *t_wit) {
   find_doms(T, sh);
   clear_scores(T, sh);
   mark_children(T, sh);
+  phase_mark(sh, 5);
 }
 
 __device__ Task make_task(const SearchParams &P, Sh &sh, uint32_t *dyn,
@@ -1006,6 +1026,9 @@ step_test_kernel(SearchParams P) {
   if (threadIdx.x == 0) {
     sh.kl = P.t_kl[ti];
     sh.bytes = 0;
+    for (int i = 0; i < 8; i++) sh.ph[i] = 0;
+    sh.r12 = sh.r3 = 0;
+    sh.t_ph = clock64();
   }
   __syncthreads();
   Task T = make_task(P, sh, dyn, ti);
@@ -1197,6 +1220,9 @@ search_kernel(SearchParams P) {
     sh.have = 0;
     sh.stop = 0;
     sh.bytes = 0;
+    for (int i = 0; i < 8; i++) sh.ph[i] = 0;
+    sh.r12 = sh.r3 = 0;
+    sh.t_ph = clock64();
   }
   __syncthreads();
   Task T;
@@ -1268,10 +1294,12 @@ search_kernel(SearchParams P) {
         __syncthreads();
         continue;
       }
+      phase_mark(sh, 7);
       T = make_task(P, sh, dyn, cta);
       load_record(rec, T, sh);
       if (t == 0) sh.have = 1;
       __syncthreads();
+      phase_mark(sh, 0);
     }
     // ---------------- one step ----------------
     if (t == 0) sh.wit_pending = *(volatile uint32_t *)&P.slots[sh.slot].abort;
@@ -1354,6 +1382,7 @@ search_kernel(SearchParams P) {
         clear_aux_list(T, sh);
       }
     }
+    phase_mark(sh, 6);
     if (t == 0) {
       finish_tasks(P, sh.slot, (long long)pushed - 1);
       Slot *sl = P.slots + sh.slot;
@@ -1451,6 +1480,10 @@ search_kernel(SearchParams P) {
     P.stk.bot[cta] = s_bot;
     atomicAdd(&P.ctr->nodes, local_nodes);
     atomicAdd(&P.ctr->bytes, sh.bytes);
+    for (int i = 0; i < 8; i++) atomicAdd(&P.ctr->phase_cycles[i], sh.ph[i]);
+    atomicAdd(&P.ctr->r12_rounds, sh.r12);
+    atomicAdd(&P.ctr->r3_rounds, sh.r3);
+    atomicAdd(&P.ctr->steps, local_nodes);
   }
 }
 

@@ -95,6 +95,7 @@ struct scs_engine {
   uint64_t next_ticket = 1;
   uint32_t running = 0;
   uint64_t stats[SCS_STAT_COUNT] = {0};
+  uint64_t prof[16] = {0};
   std::vector<HeuWork> work;
   unsigned host_threads = 1;
   std::vector<void *> allocs;
@@ -438,6 +439,10 @@ static int slice(scs_engine *E) {
     E->prep_pending = false;
   }
   E->stats[SCS_STAT_BYTES] = hc.bytes;
+  for (int i = 0; i < 8; i++) E->prof[i] = hc.phase_cycles[i];
+  E->prof[8] = hc.r12_rounds;
+  E->prof[9] = hc.r3_rounds;
+  E->prof[10] = hc.steps;
   E->stats[SCS_STAT_D2H] += E->nslots * sizeof(Slot) + sizeof(Counters) + 8;
   E->stats[SCS_STAT_H2D] += 24;
   E->stats[SCS_STAT_NODES] = hc.nodes;
@@ -595,6 +600,12 @@ int scs_poll(scs_engine *E, scs_result *out, int max, uint32_t *h_buf,
 int scs_stats(scs_engine *E, uint64_t *out) {
   if (!E || !out) return SCS_EINVAL;
   std::copy(E->stats, E->stats + SCS_STAT_COUNT, out);
+  return 0;
+}
+
+int scs_profile(scs_engine *E, uint64_t *out) {
+  if (!E || !out) return SCS_EINVAL;
+  std::copy(E->prof, E->prof + 16, out);
   return 0;
 }
 

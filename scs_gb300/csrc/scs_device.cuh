@@ -109,6 +109,9 @@ struct Counters {
   uint32_t done_count;
   uint32_t stop;               // host asks CTAs to leave the slice
   uint32_t err_info[4];
+  // profiling: clock cycles per step phase summed over CTAs, and rounds
+  unsigned long long phase_cycles[8];  // load, mindeg+r3, r12, bounds, ustar, doms, kids, other
+  unsigned long long r12_rounds, r3_rounds, steps;
 };
 
 constexpr uint32_t ERR_SPIN = 1, ERR_POOL = 2, ERR_STACK = 4, ERR_RECORD = 8;

@@ -79,6 +79,7 @@ def lib(build_if_missing=False):
     L.scs_run.argtypes = [vp]
     L.scs_poll.argtypes = [vp, C.POINTER(Result), C.c_int, _u32p, C.c_uint32]
     L.scs_stats.argtypes = [vp, _u64p]
+    L.scs_profile.argtypes = [vp, _u64p]
     L.scs_last_error.argtypes = [vp]
     L.scs_last_error.restype = C.c_char_p
     L.scs_destroy.argtypes = [vp]
@@ -272,6 +273,13 @@ class Engine:
         arr = (C.c_uint64 * 16)()
         self._check(lib().scs_stats(self._h, arr), "scs_stats")
         return {name: int(arr[i]) for i, name in enumerate(STAT_NAMES)}
+
+    def profile(self):
+        arr = (C.c_uint64 * 16)()
+        self._check(lib().scs_profile(self._h, arr), "scs_profile")
+        names = ["load", "mindeg_rule3", "rules12", "bounds", "ustar", "doms", "children",
+                 "other", "r12_rounds", "r3_rounds", "steps"]
+        return {nm: int(arr[i]) for i, nm in enumerate(names)}
 
     # ---- test hooks ----
     def debug_prepare(self, queries, kls, ubds):
