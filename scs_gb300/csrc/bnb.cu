@@ -491,11 +491,13 @@ __device__ void bounds(Task &T, Sh &sh) {
 // ustar (src/helpers.cc:1104-1168) and dominated vertices (:545-670)
 //
 // Scores are pushed from C: for each u in C in ascending id order, every R
-// neighbour v gets += 1/dC(u) (1.0 when dC(u) == 0) into ssc[v] and
-// += 1/dC(u) (0.0 when dC(u) == 0) into dsc[v].  Each v receives its terms in
-// ascending u order -- the order the oracle sums them scanning N(v) -- so the
-// doubles are bit-identical, and the work is sum deg(C) instead of
-// sum deg(candidates).
+// neighbour v gets += 1/dC(u) (1.0 when dC(u) == 0) into ssc[v].  Each v
+// receives its terms in ascending u order -- the order the oracle sums them
+// scanning N(v) -- so the doubles are bit-identical, and the work is
+// sum deg(C) instead of sum deg(candidates).  The dominated-vertex score uses
+// the same terms except that dC(u) == 0 contributes 0; C stays connected, so
+// dC(u) == 0 happens only for |C| == 1 (the root), where that partial sum is
+// 0 and ssc is not used for it.
 // ---------------------------------------------------------------------------
 __device__ void score_candidates(Task &T, Sh &sh) {
   const int t = threadIdx.x;
@@ -511,14 +513,10 @@ __device__ void score_candidates(Task &T, Sh &sh) {
     const uint32_t u = sh.A[ci];
     const uint32_t dc = dc_of(T.W[u]);
     const double wu = dc ? __ddiv_rn(1.0, (double)dc) : 1.0;
-    const double wd = dc ? wu : 0.0;
     const uint32_t b = T.off[u], e = T.off[u + 1];
     for (uint32_t k = b + t; k < e; k += BT) {
       uint32_t nb = T.adj[k];
-      if (nb != SENT && st_of(T.W[nb]) == ST_R) {
-        T.ssc[nb] = __dadd_rn(T.ssc[nb], wu);
-        T.dsc[nb] = __dadd_rn(T.dsc[nb], wd);
-      }
+      if (nb != SENT && st_of(T.W[nb]) == ST_R) T.ssc[nb] = __dadd_rn(T.ssc[nb], wu);
     }
     __syncthreads();
   }
@@ -568,11 +566,7 @@ __device__ void choose_ustar(Task &T, Sh &sh) {
 // reset the pushed scores (candidates are exactly the R vertices with C
 // neighbours, i.e. every vertex that received a term)
 __device__ void clear_scores(Task &T, Sh &sh) {
-  for (uint32_t ci = threadIdx.x; ci < sh.ndom_cand; ci += BT) {
-    uint32_t x = T.tmp[ci];
-    T.ssc[x] = 0.0;
-    T.dsc[x] = 0.0;
-  }
+  for (uint32_t ci = threadIdx.x; ci < sh.ndom_cand; ci += BT) T.ssc[T.tmp[ci]] = 0.0;
   __syncthreads();
 }
 
@@ -586,23 +580,8 @@ __device__ uint32_t list_index(const uint32_t *list, uint32_t s, uint32_t x) {
   return lo;
 }
 
-// every live neighbour of x is u* or a neighbour of u* (marked in aux)
-__device__ bool warp_dominated(Task &T, uint32_t x) {
-  const int lane = threadIdx.x & 31;
-  uint32_t b = T.off[x], e = T.off[x + 1];
-  for (uint32_t k = b; k < e; k += 32) {
-    bool bad = false;
-    if (k + lane < e) {
-      uint32_t nb = T.adj[k + lane];
-      if (nb != SENT && live(T.W[nb]) && T.aux[nb] == 0u) bad = true;
-    }
-    if (__any_sync(0xffffffffu, bad)) return false;
-  }
-  return true;
-}
-
 __device__ void find_doms(Task &T, Sh &sh) {
-  const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+  const int t = threadIdx.x;
   const uint32_t u = sh.ustar;
   if (t == 0) {
     sh.ndoms = 0;
@@ -623,17 +602,32 @@ __device__ void find_doms(Task &T, Sh &sh) {
   }
   __syncthreads();
   // candidates (R, dC > 0) are in tmp[0..nc); necessary conditions for
-  // N_T(v) within N_T(u*)+u*: dC(v) <= dC(u*), deg_T(v) <= deg_T(u*) + 1
+  // N_T(v) within N_T(u*)+u*: dC(v) <= dC(u*), deg_T(v) <= deg_T(u*) + 1.
+  // One lane per candidate: most candidates fail at their first neighbours,
+  // so 32 candidates per warp keep many independent loads in flight.
   const uint32_t nc = sh.ndom_cand;
   const double dmax = (double)sh.dmax;
+  const bool root_c = sh.csize <= 1;  // dom partial sum is 0 when |C| == 1
   uint32_t *dom_id = T.tmp + sh.s;  // second half of tmp (s <= n)
-  for (uint32_t ci = wid; ci < nc; ci += NWARP) {
+  for (uint32_t ci = t; ci < nc; ci += BT) {
     uint32_t x = T.tmp[ci];
     if (x == u) continue;
     uint32_t wx = T.W[x];
     if (dc_of(wx) > dcu || dc_of(wx) + dr_of(wx) > degu + 1u) continue;
-    if (warp_dominated(T, x) && lane == 0) {
-      double sc = __dadd_rn(T.dsc[x], __ddiv_rn((double)dr_of(wx), dmax));
+    bool dom = true;
+    const uint32_t b = T.off[x], e = T.off[x + 1];
+    for (uint32_t k = b; k < e && dom; k += 4) {
+      const uint4 q4 = *reinterpret_cast<const uint4 *>(T.adj + k);
+      const uint32_t nb4[4] = {q4.x, q4.y, q4.z, q4.w};
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        uint32_t nb = nb4[j];
+        if (nb != SENT && live(T.W[nb]) && T.aux[nb] == 0u) dom = false;
+      }
+    }
+    if (dom) {
+      double part = root_c ? 0.0 : T.ssc[x];
+      double sc = __dadd_rn(part, __ddiv_rn((double)dr_of(wx), dmax));
       uint32_t k = atomicAdd(&sh.cnt[1], 1u);
       dom_id[k] = x;
       T.dsc2[k] = sc;

@@ -163,7 +163,9 @@ static int engine_init(scs_engine *E) {
   RC(E->dalloc(&E->d_slots, E->nslots));
   SlotArrays &sa = E->sa;
   sa.stride_n = n;
-  sa.cap_adj = nnz + 3ull * n + 4;
+  // a multiple of 4 words: every slot's rows start 16-byte aligned (rows are
+  // read with 16-byte loads)
+  sa.cap_adj = (nnz + 3ull * n + 4 + 3) & ~3ull;
   sa.wit_cap = CL_CAP;
   RC(E->dalloc(&sa.loc_off, (size_t)E->nslots * (n + 1), false));
   RC(E->dalloc(&sa.loc_adj, (size_t)E->nslots * sa.cap_adj, false));
