@@ -163,6 +163,7 @@ __device__ __forceinline__ void phase_mark(Sh &sh, int which) {
 struct Task {
   uint32_t *W;
   uint32_t *list;
+  uint32_t *list2;  // second buffer for stable compaction
   uint32_t *aux;
   uint32_t *tmp;
   double *ssc;   // pushed ustar scores, by local id (zero between uses)
@@ -322,8 +323,60 @@ __device__ void rule3(Task &T, Sh &sh) {
 }
 
 // ---------------------------------------------------------------------------
-// rules 1/2 to a fixpoint (src/helpers.cc:970-1028), then compact the list
+// rules 1/2 to a fixpoint (src/helpers.cc:970-1028), then compact the list.
+// Synchronous rounds: round 1 checks every R entry; a later round's removals
+// can only be neighbours of the previous round's (kl is fixed within the
+// step and violation is monotone in dR), so they are detected right after
+// each degree decrement and queued (aux marks dedupe) -- each round costs
+// its removals' adjacency, not a pass over the task.
 // ---------------------------------------------------------------------------
+__device__ __forceinline__ bool r12_violates(uint32_t w, uint32_t dist,
+                                             uint32_t rules, uint32_t kl,
+                                             uint32_t h, uint32_t cs,
+                                             uint32_t ubd) {
+  uint32_t dc = dc_of(w), dr = dr_of(w);
+  if (rules & R_RED1) {
+    uint32_t a = dr + dc, b2 = dc + h - cs - 1u;
+    if (min(a, b2) <= kl) return true;
+  }
+  return (rules & R_RED2) && dist > ubd;
+}
+
+// Stable compaction of the live list into the second list buffer, keeping
+// entries whose state word satisfies keep(); swaps the buffers.
+template <class Keep>
+__device__ void compact_list(Task &T, Sh &sh, Keep keep) {
+  const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+  const uint32_t s = sh.s;
+  uint32_t out = 0;
+  for (uint32_t i0 = 0; i0 < s; i0 += BT) {
+    uint32_t i = i0 + t;
+    uint32_t x = 0;
+    bool k = false;
+    if (i < s) {
+      x = T.list[i];
+      k = keep(x);
+    }
+    unsigned m = __ballot_sync(0xffffffffu, k);
+    if (lane == 0) sh.red_u[wid] = __popc(m);
+    __syncthreads();
+    uint32_t before = 0, tot = 0;
+    for (int q = 0; q < NWARP; q++) {
+      uint32_t c = sh.red_u[q];
+      if (q < wid) before += c;
+      tot += c;
+    }
+    if (k) T.list2[out + before + __popc(m & ((1u << lane) - 1u))] = x;
+    out += tot;
+    __syncthreads();
+  }
+  uint32_t *tmpp = T.list;
+  T.list = T.list2;
+  T.list2 = tmpp;
+  if (t == 0) sh.s = out;
+  __syncthreads();
+}
+
 __device__ void rule12(Task &T, Sh &sh, bool test) {
   const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
   const uint32_t h = sh.h, rules = sh.rules;
@@ -333,81 +386,72 @@ __device__ void rule12(Task &T, Sh &sh, bool test) {
     // query's mean local degree (local CSR entries / local vertices)
     sh.bytes += 16ull * sh.s + (unsigned long long)(4.0f * sh.s * sh.mean_deg);
   }
+  uint32_t removed = 0;
   if (rules & (R_RED1 | R_RED2)) {
-    for (;;) {
-      refresh_kl(T, sh, test);
-      const uint32_t kl = sh.kl, cs = sh.csize, s = sh.s;
-      const uint32_t ubd = ubd_dev(kl, h);
-      if (t == 0) sh.cnt[1] = 0;
-      __syncthreads();
-      for (uint32_t i0 = 0; i0 < s; i0 += BT) {
-        uint32_t i = i0 + t;
-        bool rm = false;
-        uint32_t x = 0;
-        if (i < s) {
-          x = T.list[i];
-          uint32_t w = T.W[x];
-          if (st_of(w) == ST_R) {
-            uint32_t dc = dc_of(w), dr = dr_of(w);
-            if (rules & R_RED1) {
-              uint32_t a = dr + dc, b2 = dc + h - cs - 1u;
-              if (min(a, b2) <= kl) rm = true;
-            }
-            if ((rules & R_RED2) && (uint32_t)T.dist[x] > ubd) rm = true;
-          }
-        }
-        warp_append(rm, x, &sh.cnt[1], T.tmp);
+    refresh_kl(T, sh, test);
+    const uint32_t kl = sh.kl, cs = sh.csize, s = sh.s;
+    const uint32_t ubd = ubd_dev(kl, h);
+    if (t == 0) sh.cnt[1] = 0;
+    __syncthreads();
+    for (uint32_t i0 = 0; i0 < s; i0 += BT) {
+      uint32_t i = i0 + t;
+      bool rm = false;
+      uint32_t x = 0;
+      if (i < s) {
+        x = T.list[i];
+        uint32_t w = T.W[x];
+        rm = st_of(w) == ST_R && r12_violates(w, T.dist[x], rules, kl, h, cs, ubd);
+      }
+      warp_append(rm, x, &sh.cnt[1], T.tmp);
+    }
+    __syncthreads();
+    uint32_t base = 0, nr = sh.cnt[1];
+    while (nr > 0) {
+      if (t == 0) sh.r12++;
+      for (uint32_t i = base + t; i < base + nr; i += BT) {
+        uint32_t x = T.tmp[i];
+        T.W[x] = ST_X << 30;
+        T.aux[x] = 0;
       }
       __syncthreads();
-      const uint32_t nr = sh.cnt[1];
-      if (t == 0) sh.r12++;
-      if (nr == 0) break;
-      for (uint32_t i = t; i < nr; i += BT) T.W[T.tmp[i]] = ST_X << 30;
-      __syncthreads();
-      for (uint32_t ri = wid; ri < nr; ri += NWARP) {
+      for (uint32_t ri = base + wid; ri < base + nr; ri += NWARP) {
         uint32_t x = T.tmp[ri];
         uint32_t b = T.off[x], e = T.off[x + 1];
-        for (uint32_t k = b + lane; k < e; k += 32) {
-          uint32_t nb = T.adj[k];
-          if (nb != SENT && live(T.W[nb])) atomicSub(&T.W[nb], 1u);
+        for (uint32_t k = b; k < e; k += 32) {
+          bool q = false;
+          uint32_t nb = SENT;
+          if (k + lane < e) {
+            nb = T.adj[k + lane];
+            if (nb != SENT && live(T.W[nb])) {
+              uint32_t old = atomicSub(&T.W[nb], 1u);
+              uint32_t now = old - 1u;
+              if (st_of(now) == ST_R &&
+                  r12_violates(now, T.dist[nb], rules, kl, h, cs, ubd))
+                q = atomicExch(&T.aux[nb], 1u) == 0u;
+            }
+          }
+          warp_append(q, nb, &sh.cnt[1], T.tmp);
         }
       }
       __syncthreads();
+      const uint32_t tot = sh.cnt[1];
+      base += nr;
+      nr = tot - base;
+      __syncthreads();
     }
+    removed = base;
   }
-  // compact: drop removed entries, count R
-  const uint32_t s = sh.s;
-  uint32_t out = 0, nR = 0;
-  for (uint32_t i0 = 0; i0 < s; i0 += BT) {
-    uint32_t i = i0 + t;
-    uint32_t x = 0, w = 0;
-    bool keep = false;
-    if (i < s) {
-      x = T.list[i];
-      w = T.W[x];
-      keep = st_of(w) != ST_X;
-      if (!keep) T.W[x] = 0;
-      if (keep && st_of(w) == ST_R) nR++;
-    }
-    unsigned m = __ballot_sync(0xffffffffu, keep);
-    if (lane == 0) sh.red_u[wid] = __popc(m);
-    __syncthreads();
-    uint32_t before = 0, tot = 0;
-    for (int k = 0; k < NWARP; k++) {
-      uint32_t c = sh.red_u[k];
-      if (k < wid) before += c;
-      tot += c;
-    }
-    __syncthreads();
-    if (keep) T.list[out + before + __popc(m & ((1u << lane) - 1u))] = x;
-    out += tot;
-    __syncthreads();
+  if (removed) {
+    compact_list(T, sh, [&](uint32_t x) {
+      uint32_t w = T.W[x];
+      if (st_of(w) == ST_X) {
+        T.W[x] = 0;
+        return false;
+      }
+      return true;
+    });
   }
-  nR = block_sum(nR, sh);
-  if (t == 0) {
-    sh.s = out;
-    sh.nR = nR;
-  }
+  if (t == 0) sh.nR = sh.s - sh.csize;
   __syncthreads();
 }
 
@@ -856,33 +900,10 @@ __device__ void apply_include(Task &T, Sh &sh) {
   }
   __syncthreads();
   // compact the live list (drop D)
-  uint32_t out = 0;
-  for (uint32_t i0 = 0; i0 < s; i0 += BT) {
-    uint32_t i = i0 + t;
-    uint32_t x = 0;
-    bool keep = false;
-    if (i < s) {
-      x = T.list[i];
-      keep = T.W[x] != 0;
-    }
-    unsigned m = __ballot_sync(0xffffffffu, keep);
-    if (lane == 0) sh.red_u[wid] = __popc(m);
-    __syncthreads();
-    uint32_t before = 0, tot = 0;
-    for (int q = 0; q < NWARP; q++) {
-      uint32_t c = sh.red_u[q];
-      if (q < wid) before += c;
-      tot += c;
-    }
-    __syncthreads();
-    if (keep) T.list[out + before + __popc(m & ((1u << lane) - 1u))] = x;
-    out += tot;
-    __syncthreads();
-  }
+  if (k) compact_list(T, sh, [&](uint32_t x) { return T.W[x] != 0; });
   if (t == 0) {
     if (sh.csize < CL_CAP) sh.cl[sh.csize] = sh.ustar;
     sh.csize += 1;
-    sh.s = out;
   }
   __syncthreads();
 }
@@ -968,7 +989,8 @@ __device__ Task make_task(const SearchParams &P, Sh &sh, uint32_t *dyn,
   const uint32_t slot = sh.slot;
   const size_t st = P.scr.stride;
   T.W = (sh.n_local <= P.nw_smem) ? dyn : P.scr.word + (size_t)cta * st;
-  T.list = P.scr.list + (size_t)cta * st;
+  T.list = P.scr.list + (size_t)cta * 2 * st;
+  T.list2 = T.list + st;
   T.aux = P.scr.aux + (size_t)cta * st;
   T.tmp = P.scr.tmp + (size_t)cta * 2 * st;
   T.ssc = P.scr.dsc + (size_t)cta * 3 * st;

@@ -213,7 +213,7 @@ static int engine_init(scs_engine *E) {
   Scratch &sc = E->scr;
   sc.stride = n + 4;
   RC(E->dalloc(&sc.word, (size_t)E->grid * sc.stride));
-  RC(E->dalloc(&sc.list, (size_t)E->grid * sc.stride, false));
+  RC(E->dalloc(&sc.list, (size_t)E->grid * 2 * sc.stride, false));
   RC(E->dalloc(&sc.aux, (size_t)E->grid * sc.stride));
   RC(E->dalloc(&sc.tmp, (size_t)E->grid * 2 * sc.stride, false));
   RC(E->dalloc(&sc.dsc, (size_t)E->grid * 3 * sc.stride));  // zeroed: scores
