@@ -324,11 +324,8 @@ __device__ void rule3(Task &T, Sh &sh) {
 
 // ---------------------------------------------------------------------------
 // rules 1/2 to a fixpoint (src/helpers.cc:970-1028), then compact the list.
-// Synchronous rounds: round 1 checks every R entry; a later round's removals
-// can only be neighbours of the previous round's (kl is fixed within the
-// step and violation is monotone in dR), so they are detected right after
-// each degree decrement and queued (aux marks dedupe) -- each round costs
-// its removals' adjacency, not a pass over the task.
+// Synchronous rounds, each a pass over the live entries; the list is
+// compacted only when something was removed, and |R| = s - |C| afterwards.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ bool r12_violates(uint32_t w, uint32_t dist,
                                              uint32_t rules, uint32_t kl,
@@ -388,58 +385,41 @@ __device__ void rule12(Task &T, Sh &sh, bool test) {
   }
   uint32_t removed = 0;
   if (rules & (R_RED1 | R_RED2)) {
-    refresh_kl(T, sh, test);
-    const uint32_t kl = sh.kl, cs = sh.csize, s = sh.s;
-    const uint32_t ubd = ubd_dev(kl, h);
-    if (t == 0) sh.cnt[1] = 0;
-    __syncthreads();
-    for (uint32_t i0 = 0; i0 < s; i0 += BT) {
-      uint32_t i = i0 + t;
-      bool rm = false;
-      uint32_t x = 0;
-      if (i < s) {
-        x = T.list[i];
-        uint32_t w = T.W[x];
-        rm = st_of(w) == ST_R && r12_violates(w, T.dist[x], rules, kl, h, cs, ubd);
-      }
-      warp_append(rm, x, &sh.cnt[1], T.tmp);
-    }
-    __syncthreads();
-    uint32_t base = 0, nr = sh.cnt[1];
-    while (nr > 0) {
-      if (t == 0) sh.r12++;
-      for (uint32_t i = base + t; i < base + nr; i += BT) {
-        uint32_t x = T.tmp[i];
-        T.W[x] = ST_X << 30;
-        T.aux[x] = 0;
+    for (;;) {
+      refresh_kl(T, sh, test);
+      const uint32_t kl = sh.kl, cs = sh.csize, s = sh.s;
+      const uint32_t ubd = ubd_dev(kl, h);
+      if (t == 0) sh.cnt[1] = 0;
+      __syncthreads();
+      for (uint32_t i0 = 0; i0 < s; i0 += BT) {
+        uint32_t i = i0 + t;
+        bool rm = false;
+        uint32_t x = 0;
+        if (i < s) {
+          x = T.list[i];
+          uint32_t w = T.W[x];
+          rm = st_of(w) == ST_R && r12_violates(w, T.dist[x], rules, kl, h, cs, ubd);
+        }
+        warp_append(rm, x, &sh.cnt[1], T.tmp);
       }
       __syncthreads();
-      for (uint32_t ri = base + wid; ri < base + nr; ri += NWARP) {
+      const uint32_t nr = sh.cnt[1];
+      if (nr == 0) break;
+      if (t == 0) sh.r12++;
+      removed += nr;
+      for (uint32_t i = t; i < nr; i += BT) T.W[T.tmp[i]] = ST_X << 30;
+      __syncthreads();
+      // neighbours lose one R neighbour each (non-returning reductions)
+      for (uint32_t ri = wid; ri < nr; ri += NWARP) {
         uint32_t x = T.tmp[ri];
         uint32_t b = T.off[x], e = T.off[x + 1];
-        for (uint32_t k = b; k < e; k += 32) {
-          bool q = false;
-          uint32_t nb = SENT;
-          if (k + lane < e) {
-            nb = T.adj[k + lane];
-            if (nb != SENT && live(T.W[nb])) {
-              uint32_t old = atomicSub(&T.W[nb], 1u);
-              uint32_t now = old - 1u;
-              if (st_of(now) == ST_R &&
-                  r12_violates(now, T.dist[nb], rules, kl, h, cs, ubd))
-                q = atomicExch(&T.aux[nb], 1u) == 0u;
-            }
-          }
-          warp_append(q, nb, &sh.cnt[1], T.tmp);
+        for (uint32_t k = b + lane; k < e; k += 32) {
+          uint32_t nb = T.adj[k];
+          if (nb != SENT && live(T.W[nb])) atomicSub(&T.W[nb], 1u);
         }
       }
       __syncthreads();
-      const uint32_t tot = sh.cnt[1];
-      base += nr;
-      nr = tot - base;
-      __syncthreads();
     }
-    removed = base;
   }
   if (removed) {
     compact_list(T, sh, [&](uint32_t x) {
