@@ -54,6 +54,8 @@ struct Sh {
   uint32_t A[CL_CAP];
   uint32_t B[CL_CAP];
   uint32_t hist[CL_CAP + 1];
+  double wtab[64];   // 1/dC of the r-th smallest C vertex (ustar terms)
+  uint32_t stride;   // per-CTA scratch stride (words)
   uint32_t kid_len[MAX_DOMS + 2];
   unsigned long long kid_dst[MAX_DOMS + 2];
   unsigned long long kid_pool[MAX_DOMS + 2];
@@ -160,6 +162,10 @@ __device__ __forceinline__ void phase_mark(Sh &sh, int which) {
   }
 }
 
+// In-place exclusive scan of a[0..len) (any memory); writes the total to
+// a[len] and returns it.  All threads call.
+__device__ uint32_t block_excl_scan_bt(uint32_t *a, uint32_t len, Sh &sh);
+
 struct Task {
   uint32_t *W;
   uint32_t *list;
@@ -176,6 +182,82 @@ struct Task {
   uint32_t *witness;
   Slot *slot;
 };
+
+__device__ uint32_t block_excl_scan_bt(uint32_t *a, uint32_t len, Sh &sh) {
+  const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+  uint32_t running = 0;
+  for (uint32_t base = 0; base < len; base += BT) {
+    uint32_t i = base + t;
+    uint32_t v = i < len ? a[i] : 0;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) sh.red_u[wid] = x;
+    __syncthreads();
+    uint32_t woff = 0, tot = 0;
+    for (int q = 0; q < NWARP; q++) {
+      uint32_t c = sh.red_u[q];
+      if (q < wid) woff += c;
+      tot += c;
+    }
+    if (i < len) a[i] = running + woff + x - v;
+    running += tot;
+    __syncthreads();
+  }
+  if (t == 0) a[len] = running;
+  __syncthreads();
+  return running;
+}
+
+// Visit the padded adjacency rows of ids[0..cnt) as one flat range of 16-byte
+// units split evenly over the CTA's threads (each thread a contiguous range),
+// calling f(r, nb) for every neighbour nb != SENT of ids[r].  pre needs
+// cnt+1 words of scratch.  All threads call.
+template <class F>
+__device__ void for_rows_balanced(Task &T, Sh &sh, const uint32_t *ids,
+                                  uint32_t cnt, uint32_t *pre, F f) {
+  const int t = threadIdx.x;
+  for (uint32_t i = t; i < cnt; i += BT) {
+    uint32_t x = ids[i];
+    pre[i] = (T.off[x + 1] - T.off[x]) >> 2;
+  }
+  __syncthreads();
+  const uint32_t total = block_excl_scan_bt(pre, cnt, sh);
+  const uint32_t per = (total + BT - 1) / BT;
+  uint32_t beg = min(total, t * per), end = min(total, beg + per);
+  if (beg < end) {
+    // row containing unit beg: last r with pre[r] <= beg
+    uint32_t lo = 0, hi = cnt;
+    while (hi - lo > 1) {
+      uint32_t mid = (lo + hi) >> 1;
+      if (pre[mid] <= beg) lo = mid;
+      else hi = mid;
+    }
+    uint32_t r = lo;
+    uint32_t row_end = pre[r + 1];
+    uint32_t x = ids[r];
+    const uint32_t *rowp = T.adj + T.off[x];
+    uint32_t rbeg = pre[r];
+    for (uint32_t u = beg; u < end; u++) {
+      while (u >= row_end) {
+        r++;
+        row_end = pre[r + 1];
+        rbeg = pre[r];
+        x = ids[r];
+        rowp = T.adj + T.off[x];
+      }
+      const uint4 q4 = *reinterpret_cast<const uint4 *>(rowp + 4 * (u - rbeg));
+      if (q4.x != SENT) f(r, q4.x);
+      if (q4.y != SENT) f(r, q4.y);
+      if (q4.z != SENT) f(r, q4.z);
+      if (q4.w != SENT) f(r, q4.w);
+    }
+  }
+  __syncthreads();
+}
 
 // ---------------------------------------------------------------------------
 // load a record into the state words / live list / C list
@@ -409,16 +491,11 @@ __device__ void rule12(Task &T, Sh &sh, bool test) {
       removed += nr;
       for (uint32_t i = t; i < nr; i += BT) T.W[T.tmp[i]] = ST_X << 30;
       __syncthreads();
-      // neighbours lose one R neighbour each (non-returning reductions)
-      for (uint32_t ri = wid; ri < nr; ri += NWARP) {
-        uint32_t x = T.tmp[ri];
-        uint32_t b = T.off[x], e = T.off[x + 1];
-        for (uint32_t k = b + lane; k < e; k += 32) {
-          uint32_t nb = T.adj[k];
-          if (nb != SENT && live(T.W[nb])) atomicSub(&T.W[nb], 1u);
-        }
-      }
-      __syncthreads();
+      // neighbours lose one R neighbour each (non-returning reductions), the
+      // removed rows spread evenly over the threads
+      for_rows_balanced(T, sh, T.tmp, nr, T.tmp + sh.stride, [&](uint32_t, uint32_t nb) {
+        if (live(T.W[nb])) atomicSub(&T.W[nb], 1u);
+      });
     }
   }
   if (removed) {
@@ -533,6 +610,33 @@ __device__ void score_candidates(Task &T, Sh &sh) {
     sh.A[r] = vi;
   }
   __syncthreads();
+  if (cs <= 64) {
+    // every C row at once: candidate v collects a mask of its C neighbours
+    // (bit r = r-th smallest C id); one thread per candidate then sums the
+    // terms in bit order = ascending neighbour order, as the oracle does
+    for (uint32_t r = t; r < cs; r += BT) {
+      uint32_t dc = dc_of(T.W[sh.A[r]]);
+      sh.wtab[r] = dc ? __ddiv_rn(1.0, (double)dc) : 1.0;
+    }
+    unsigned long long *mask = reinterpret_cast<unsigned long long *>(T.ssc);
+    for_rows_balanced(T, sh, sh.A, cs, T.tmp + sh.stride, [&](uint32_t r, uint32_t nb) {
+      if (st_of(T.W[nb]) == ST_R) atomicOr(&mask[nb], 1ull << r);
+    });
+    const uint32_t nc = sh.cnt[0];
+    for (uint32_t ci = t; ci < nc; ci += BT) {
+      uint32_t x = T.tmp[ci];
+      unsigned long long m = mask[x];
+      double sc = 0.0;
+      while (m) {
+        int r = __ffsll((long long)m) - 1;
+        m &= m - 1;
+        sc = __dadd_rn(sc, sh.wtab[r]);
+      }
+      T.ssc[x] = sc;  // the mask word becomes the score
+    }
+    __syncthreads();
+    return;
+  }
   for (uint32_t ci = 0; ci < cs; ci++) {
     const uint32_t u = sh.A[ci];
     const uint32_t dc = dc_of(T.W[u]);
@@ -982,6 +1086,8 @@ __device__ Task make_task(const SearchParams &P, Sh &sh, uint32_t *dyn,
   T.gid = P.sa.loc_gid + (size_t)slot * P.sa.stride_n;
   T.witness = P.sa.witness + (size_t)slot * P.sa.wit_cap;
   T.slot = P.slots + slot;
+  if (threadIdx.x == 0) sh.stride = (uint32_t)st;
+  __syncthreads();
   return T;
 }
 
