@@ -31,19 +31,31 @@ def _deps_mtime():
 
 
 def lib_path():
-    return os.path.join(OUT, LIB)
+    return os.environ.get("SCS_LIB") or os.path.join(OUT, LIB)
 
 
-def build(verbose=False, force=False):
+def build(verbose=False, force=False, out_dir=None, defines=()):
+    """Build into out_dir (default scs_gb300/_lib) with extra -D defines."""
+    global OUT
+    saved = OUT
+    if out_dir:
+        OUT = out_dir
+    try:
+        return _build(verbose, force, list(defines))
+    finally:
+        OUT = saved
+
+
+def _build(verbose, force, defines):
     os.makedirs(OUT, exist_ok=True)
-    out = lib_path()
-    if not force and os.path.exists(out) and os.path.getmtime(out) >= _deps_mtime():
+    out = os.path.join(OUT, LIB)
+    if not force and not defines and os.path.exists(out) and os.path.getmtime(out) >= _deps_mtime():
         return out
     objdir = os.path.join(OUT, "obj")
     os.makedirs(objdir, exist_ok=True)
     cmds = []
     for f in CU:
-        cmds.append([nvcc(), *ARCH, "-O3", "-std=c++17", "-lineinfo",
+        cmds.append([nvcc(), *ARCH, "-O3", "-std=c++17", "-lineinfo", *defines,
                      "-Xcompiler", "-fPIC", "-c", os.path.join(CSRC, f),
                      "-o", os.path.join(objdir, f + ".o")])
     for f in CXX:

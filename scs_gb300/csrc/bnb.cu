@@ -25,6 +25,14 @@
 namespace scs {
 
 constexpr int BT = SEARCH_THREADS;
+
+// implementation switches (both variants are exact; chosen by measurement)
+#ifndef SCS_R12_BALANCED
+#define SCS_R12_BALANCED 0
+#endif
+#ifndef SCS_MASK_SCORES
+#define SCS_MASK_SCORES 1
+#endif
 constexpr int NWARP = BT / 32;
 
 struct Sh {
@@ -491,11 +499,22 @@ __device__ void rule12(Task &T, Sh &sh, bool test) {
       removed += nr;
       for (uint32_t i = t; i < nr; i += BT) T.W[T.tmp[i]] = ST_X << 30;
       __syncthreads();
-      // neighbours lose one R neighbour each (non-returning reductions), the
-      // removed rows spread evenly over the threads
+      // neighbours lose one R neighbour each (non-returning reductions)
+#if SCS_R12_BALANCED
       for_rows_balanced(T, sh, T.tmp, nr, T.tmp + sh.stride, [&](uint32_t, uint32_t nb) {
         if (live(T.W[nb])) atomicSub(&T.W[nb], 1u);
       });
+#else
+      for (uint32_t ri = wid; ri < nr; ri += NWARP) {
+        uint32_t x = T.tmp[ri];
+        uint32_t b = T.off[x], e = T.off[x + 1];
+        for (uint32_t k = b + lane; k < e; k += 32) {
+          uint32_t nb = T.adj[k];
+          if (nb != SENT && live(T.W[nb])) atomicSub(&T.W[nb], 1u);
+        }
+      }
+      __syncthreads();
+#endif
     }
   }
   if (removed) {
@@ -610,7 +629,7 @@ __device__ void score_candidates(Task &T, Sh &sh) {
     sh.A[r] = vi;
   }
   __syncthreads();
-  if (cs <= 64) {
+  if (SCS_MASK_SCORES && cs <= 64) {
     // every C row at once: candidate v collects a mask of its C neighbours
     // (bit r = r-th smallest C id); one thread per candidate then sums the
     // terms in bit order = ascending neighbour order, as the oracle does
