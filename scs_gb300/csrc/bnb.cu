@@ -31,7 +31,7 @@ constexpr int BT = SEARCH_THREADS;
 #define SCS_R12_BALANCED 0
 #endif
 #ifndef SCS_MASK_SCORES
-#define SCS_MASK_SCORES 1
+#define SCS_MASK_SCORES 0
 #endif
 constexpr int NWARP = BT / 32;
 
@@ -51,6 +51,8 @@ struct Sh {
   unsigned long long ph[8];  // clock cycles per phase (thread 0)
   unsigned long long t_ph;   // start of the current phase
   unsigned long long r12, r3;
+  unsigned long long sub[4];   // rule12: check passes, removal scans, compaction, -
+  unsigned long long cnt4[4];  // removed vertices, removed row words, survivors, -
   float mean_deg;            // local CSR entries per local vertex (this query)
   int have;
   int stop;
@@ -479,6 +481,7 @@ __device__ void rule12(Task &T, Sh &sh, bool test) {
       refresh_kl(T, sh, test);
       const uint32_t kl = sh.kl, cs = sh.csize, s = sh.s;
       const uint32_t ubd = ubd_dev(kl, h);
+      unsigned long long c0 = clock64();
       if (t == 0) sh.cnt[1] = 0;
       __syncthreads();
       for (uint32_t i0 = 0; i0 < s; i0 += BT) {
@@ -494,8 +497,14 @@ __device__ void rule12(Task &T, Sh &sh, bool test) {
       }
       __syncthreads();
       const uint32_t nr = sh.cnt[1];
+      if (t == 0) sh.sub[0] += clock64() - c0;
       if (nr == 0) break;
-      if (t == 0) sh.r12++;
+      c0 = clock64();
+      if (t == 0) {
+        sh.r12++;
+        sh.cnt4[0] += nr;
+        sh.cnt4[2] += s - nr;
+      }
       removed += nr;
       for (uint32_t i = t; i < nr; i += BT) T.W[T.tmp[i]] = ST_X << 30;
       __syncthreads();
@@ -508,6 +517,7 @@ __device__ void rule12(Task &T, Sh &sh, bool test) {
       for (uint32_t ri = wid; ri < nr; ri += NWARP) {
         uint32_t x = T.tmp[ri];
         uint32_t b = T.off[x], e = T.off[x + 1];
+        if (lane == 0) atomicAdd(&sh.cnt4[1], (unsigned long long)(e - b));
         for (uint32_t k = b + lane; k < e; k += 32) {
           uint32_t nb = T.adj[k];
           if (nb != SENT && live(T.W[nb])) atomicSub(&T.W[nb], 1u);
@@ -515,8 +525,10 @@ __device__ void rule12(Task &T, Sh &sh, bool test) {
       }
       __syncthreads();
 #endif
+      if (t == 0) sh.sub[1] += clock64() - c0;
     }
   }
+  unsigned long long c1 = clock64();
   if (removed) {
     compact_list(T, sh, [&](uint32_t x) {
       uint32_t w = T.W[x];
@@ -527,7 +539,10 @@ __device__ void rule12(Task &T, Sh &sh, bool test) {
       return true;
     });
   }
-  if (t == 0) sh.nR = sh.s - sh.csize;
+  if (t == 0) {
+    sh.nR = sh.s - sh.csize;
+    sh.sub[2] += clock64() - c1;
+  }
   __syncthreads();
 }
 
@@ -1148,6 +1163,7 @@ step_test_kernel(SearchParams P) {
     sh.kl = P.t_kl[ti];
     sh.bytes = 0;
     for (int i = 0; i < 8; i++) sh.ph[i] = 0;
+    for (int i = 0; i < 4; i++) sh.sub[i] = sh.cnt4[i] = 0;
     sh.r12 = sh.r3 = 0;
     sh.t_ph = clock64();
   }
@@ -1342,6 +1358,7 @@ search_kernel(SearchParams P) {
     sh.stop = 0;
     sh.bytes = 0;
     for (int i = 0; i < 8; i++) sh.ph[i] = 0;
+    for (int i = 0; i < 4; i++) sh.sub[i] = sh.cnt4[i] = 0;
     sh.r12 = sh.r3 = 0;
     sh.t_ph = clock64();
   }
@@ -1605,6 +1622,10 @@ search_kernel(SearchParams P) {
     atomicAdd(&P.ctr->r12_rounds, sh.r12);
     atomicAdd(&P.ctr->r3_rounds, sh.r3);
     atomicAdd(&P.ctr->steps, local_nodes);
+    for (int i = 0; i < 4; i++) {
+      atomicAdd(&P.ctr->sub_cycles[i], sh.sub[i]);
+      atomicAdd(&P.ctr->sub_counts[i], sh.cnt4[i]);
+    }
   }
 }
 

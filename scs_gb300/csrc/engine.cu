@@ -445,6 +445,11 @@ static int slice(scs_engine *E) {
   E->prof[8] = hc.r12_rounds;
   E->prof[9] = hc.r3_rounds;
   E->prof[10] = hc.steps;
+  for (int i = 0; i < 3; i++) {
+    E->prof[11 + i] = hc.sub_cycles[i];
+  }
+  E->prof[14] = hc.sub_counts[0];
+  E->prof[15] = hc.sub_counts[1];
   E->stats[SCS_STAT_D2H] += E->nslots * sizeof(Slot) + sizeof(Counters) + 8;
   E->stats[SCS_STAT_H2D] += 24;
   E->stats[SCS_STAT_NODES] = hc.nodes;
