@@ -33,6 +33,9 @@ constexpr int BT = SEARCH_THREADS;
 #ifndef SCS_MASK_SCORES
 #define SCS_MASK_SCORES 0
 #endif
+#ifndef SCS_ROW_UNROLL
+#define SCS_ROW_UNROLL 4
+#endif
 constexpr int NWARP = BT / 32;
 
 struct Sh {
@@ -267,6 +270,26 @@ __device__ void for_rows_balanced(Task &T, Sh &sh, const uint32_t *ids,
     }
   }
   __syncthreads();
+}
+
+// Warp-cooperative scan of one padded adjacency row with SCS_ROW_UNROLL
+// independent 128-byte loads in flight (the scans are latency-bound: one load
+// at a time left the SMs nearly idle).  f(nb) runs for every nb != SENT.
+template <class F>
+__device__ __forceinline__ void warp_row_scan(const Task &T, uint32_t x, F f) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t b = T.off[x], e = T.off[x + 1];
+  for (uint32_t k0 = b; k0 < e; k0 += 32 * SCS_ROW_UNROLL) {
+    uint32_t nb[SCS_ROW_UNROLL];
+#pragma unroll
+    for (int j = 0; j < SCS_ROW_UNROLL; j++) {
+      uint32_t k = k0 + 32 * j + lane;
+      nb[j] = k < e ? T.adj[k] : SENT;
+    }
+#pragma unroll
+    for (int j = 0; j < SCS_ROW_UNROLL; j++)
+      if (nb[j] != SENT) f(nb[j]);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -516,12 +539,10 @@ __device__ void rule12(Task &T, Sh &sh, bool test) {
 #else
       for (uint32_t ri = wid; ri < nr; ri += NWARP) {
         uint32_t x = T.tmp[ri];
-        uint32_t b = T.off[x], e = T.off[x + 1];
-        if (lane == 0) atomicAdd(&sh.cnt4[1], (unsigned long long)(e - b));
-        for (uint32_t k = b + lane; k < e; k += 32) {
-          uint32_t nb = T.adj[k];
-          if (nb != SENT && live(T.W[nb])) atomicSub(&T.W[nb], 1u);
-        }
+        if (lane == 0) atomicAdd(&sh.cnt4[1], (unsigned long long)(T.off[x + 1] - T.off[x]));
+        warp_row_scan(T, x, [&](uint32_t nb) {
+          if (live(T.W[nb])) atomicSub(&T.W[nb], 1u);
+        });
       }
       __syncthreads();
 #endif
@@ -676,9 +697,17 @@ __device__ void score_candidates(Task &T, Sh &sh) {
     const uint32_t dc = dc_of(T.W[u]);
     const double wu = dc ? __ddiv_rn(1.0, (double)dc) : 1.0;
     const uint32_t b = T.off[u], e = T.off[u + 1];
-    for (uint32_t k = b + t; k < e; k += BT) {
-      uint32_t nb = T.adj[k];
-      if (nb != SENT && st_of(T.W[nb]) == ST_R) T.ssc[nb] = __dadd_rn(T.ssc[nb], wu);
+    for (uint32_t k0 = b; k0 < e; k0 += BT * SCS_ROW_UNROLL) {
+      uint32_t nb[SCS_ROW_UNROLL];
+#pragma unroll
+      for (int j = 0; j < SCS_ROW_UNROLL; j++) {
+        uint32_t k = k0 + BT * j + t;
+        nb[j] = k < e ? T.adj[k] : SENT;
+      }
+#pragma unroll
+      for (int j = 0; j < SCS_ROW_UNROLL; j++)
+        if (nb[j] != SENT && st_of(T.W[nb[j]]) == ST_R)
+          T.ssc[nb[j]] = __dadd_rn(T.ssc[nb[j]], wu);
     }
     __syncthreads();
   }
