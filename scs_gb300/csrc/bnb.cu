@@ -34,7 +34,7 @@ constexpr int BT = SEARCH_THREADS;
 #define SCS_MASK_SCORES 0
 #endif
 #ifndef SCS_ROW_UNROLL
-#define SCS_ROW_UNROLL 4
+#define SCS_ROW_UNROLL 8
 #endif
 constexpr int NWARP = BT / 32;
 
@@ -284,6 +284,25 @@ __device__ __forceinline__ void warp_row_scan(const Task &T, uint32_t x, F f) {
 #pragma unroll
     for (int j = 0; j < SCS_ROW_UNROLL; j++) {
       uint32_t k = k0 + 32 * j + lane;
+      nb[j] = k < e ? T.adj[k] : SENT;
+    }
+#pragma unroll
+    for (int j = 0; j < SCS_ROW_UNROLL; j++)
+      if (nb[j] != SENT) f(nb[j]);
+  }
+}
+
+// Block-wide scan of one padded row (all threads), SCS_ROW_UNROLL loads in
+// flight per thread.
+template <class F>
+__device__ __forceinline__ void block_row_scan(const Task &T, uint32_t x, F f) {
+  const int t = threadIdx.x;
+  const uint32_t b = T.off[x], e = T.off[x + 1];
+  for (uint32_t k0 = b; k0 < e; k0 += BT * SCS_ROW_UNROLL) {
+    uint32_t nb[SCS_ROW_UNROLL];
+#pragma unroll
+    for (int j = 0; j < SCS_ROW_UNROLL; j++) {
+      uint32_t k = k0 + BT * j + t;
       nb[j] = k < e ? T.adj[k] : SENT;
     }
 #pragma unroll
@@ -783,14 +802,10 @@ __device__ void find_doms(Task &T, Sh &sh) {
   const uint32_t wu = T.W[u];
   const uint32_t degu = dc_of(wu) + dr_of(wu), dcu = dc_of(wu);
   // mark N_T(u*) and u*
-  {
-    uint32_t b = T.off[u], e = T.off[u + 1];
-    for (uint32_t k = b + t; k < e; k += BT) {
-      uint32_t nb = T.adj[k];
-      if (nb != SENT && live(T.W[nb])) T.aux[nb] = 1u;
-    }
-    if (t == 0) T.aux[u] = 1u;
-  }
+  block_row_scan(T, u, [&](uint32_t nb) {
+    if (live(T.W[nb])) T.aux[nb] = 1u;
+  });
+  if (t == 0) T.aux[u] = 1u;
   __syncthreads();
   // candidates (R, dC > 0) are in tmp[0..nc); necessary conditions for
   // N_T(v) within N_T(u*)+u*: dC(v) <= dC(u*), deg_T(v) <= deg_T(u*) + 1.
@@ -807,12 +822,14 @@ __device__ void find_doms(Task &T, Sh &sh) {
     if (dc_of(wx) > dcu || dc_of(wx) + dr_of(wx) > degu + 1u) continue;
     bool dom = true;
     const uint32_t b = T.off[x], e = T.off[x + 1];
-    for (uint32_t k = b; k < e && dom; k += 4) {
+    for (uint32_t k = b; k < e && dom; k += 8) {
       const uint4 q4 = *reinterpret_cast<const uint4 *>(T.adj + k);
-      const uint32_t nb4[4] = {q4.x, q4.y, q4.z, q4.w};
+      const uint4 r4 = k + 4 < e ? *reinterpret_cast<const uint4 *>(T.adj + k + 4)
+                                 : make_uint4(SENT, SENT, SENT, SENT);
+      const uint32_t nb8[8] = {q4.x, q4.y, q4.z, q4.w, r4.x, r4.y, r4.z, r4.w};
 #pragma unroll
-      for (int j = 0; j < 4; j++) {
-        uint32_t nb = nb4[j];
+      for (int j = 0; j < 8; j++) {
+        uint32_t nb = nb8[j];
         if (nb != SENT && live(T.W[nb]) && T.aux[nb] == 0u) dom = false;
       }
     }
@@ -826,14 +843,8 @@ __device__ void find_doms(Task &T, Sh &sh) {
   }
   __syncthreads();
   // clear marks
-  {
-    uint32_t b = T.off[u], e = T.off[u + 1];
-    for (uint32_t k = b + t; k < e; k += BT) {
-      uint32_t nb = T.adj[k];
-      if (nb != SENT) T.aux[nb] = 0u;
-    }
-    if (t == 0) T.aux[u] = 0u;
-  }
+  block_row_scan(T, u, [&](uint32_t nb) { T.aux[nb] = 0u; });
+  if (t == 0) T.aux[u] = 0u;
   __syncthreads();
   const uint32_t nd = sh.cnt[1];
   const uint32_t k = min(nd, min(sh.ldoms, (uint32_t)MAX_DOMS));
@@ -909,11 +920,9 @@ __device__ void mark_children(Task &T, Sh &sh) {
   // adjacency bits: warp per marked vertex
   for (uint32_t j = wid; j <= k; j += NWARP) {
     uint32_t v = j == 0 ? sh.ustar : sh.doms[j - 1];
-    uint32_t b = T.off[v], e = T.off[v + 1];
-    for (uint32_t q = b + lane; q < e; q += 32) {
-      uint32_t nb = T.adj[q];
-      if (nb != SENT && live(T.W[nb])) atomicOr(&T.aux[nb], 1u << j);
-    }
+    warp_row_scan(T, v, [&](uint32_t nb) {
+      if (live(T.W[nb])) atomicOr(&T.aux[nb], 1u << j);
+    });
   }
   __syncthreads();
   if (t == 0) {
