@@ -33,6 +33,9 @@ constexpr int BT = SEARCH_THREADS;
 #ifndef SCS_MASK_SCORES
 #define SCS_MASK_SCORES 0
 #endif
+#ifndef SCS_R12_RECOUNT
+#define SCS_R12_RECOUNT 1
+#endif
 #ifndef SCS_ROW_UNROLL
 #define SCS_ROW_UNROLL 8
 #endif
@@ -550,6 +553,22 @@ __device__ void rule12(Task &T, Sh &sh, bool test) {
       removed += nr;
       for (uint32_t i = t; i < nr; i += BT) T.W[T.tmp[i]] = ST_X << 30;
       __syncthreads();
+      if (SCS_R12_RECOUNT && s - nr < nr) {
+        // burst: fewer survivors than removals -- recount each survivor's R
+        // neighbours (exact, cost sum deg(survivors) < sum deg(removed))
+        for (uint32_t i = wid; i < s; i += NWARP) {
+          const uint32_t y = T.list[i];
+          const uint32_t wy = T.W[y];
+          if (!live(wy)) continue;
+          uint32_t c = 0;
+          warp_row_scan(T, y, [&](uint32_t nb) { c += st_of(T.W[nb]) == ST_R; });
+          c = warp_sum(c);
+          if (lane == 0) T.W[y] = (wy & ~DMASK) | c;
+        }
+        __syncthreads();
+        if (t == 0) sh.sub[1] += clock64() - c0;
+        continue;
+      }
       // neighbours lose one R neighbour each (non-returning reductions)
 #if SCS_R12_BALANCED
       for_rows_balanced(T, sh, T.tmp, nr, T.tmp + sh.stride, [&](uint32_t, uint32_t nb) {
