@@ -1,0 +1,55 @@
+"""Failure paths, driven from the host (no GPU fault, trap or hang): the
+search budget (the reference's level cap, Overtime=1), task-store overflow
+(the reference's buffer overflow, Overtime=2) and malformed queries."""
+import json
+import os
+
+import pytest
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _gold_hard(k):
+    g = json.load(open(os.path.join(GOLD, "answers_chunglu_n4000.json")))["queries"]
+    return [q for q in g if not q["heu_hit"]][:k]
+
+
+def test_search_budget_reports_timeout(chunglu_small):
+    from scs_gb300.engine import TIMEOUT, DONE, Engine
+    eng = Engine(graph=chunglu_small, limit_queries=8, node_budget=40,
+                 stack_words=1 << 22, pool_words=1 << 24)
+    rows = [(g["l"], g["h"], g["q"], g["heur"], g["limit_doms"]) for g in _gold_hard(4)]
+    res = eng.solve(rows)
+    assert any(r["status"] == TIMEOUT for r in res)
+    for g, r in zip(_gold_hard(4), res):
+        assert r["status"] in (TIMEOUT, DONE)
+        assert r["kl_heuristic"] <= r["degree"] <= max(g["degree"], r["kl_heuristic"])
+        assert r["nodes"] >= 1
+    # the engine keeps working after stopped queries
+    again = eng.solve(rows[:1])
+    assert again[0]["status"] in (TIMEOUT, DONE)
+    eng.close()
+
+
+def test_task_store_overflow_reports_capacity(chunglu_small):
+    from scs_gb300.engine import CAPACITY, DONE, Engine
+    # stacks and pool too small for the 4000-vertex root task records
+    eng = Engine(graph=chunglu_small, limit_queries=4, stack_words=4096, pool_words=1 << 14)
+    rows = [(g["l"], g["h"], g["q"], g["heur"], g["limit_doms"]) for g in _gold_hard(2)]
+    res = eng.solve(rows)
+    assert all(r["status"] in (CAPACITY, DONE) for r in res)
+    assert any(r["status"] == CAPACITY for r in res)
+    for r in res:
+        assert r["degree"] >= r["kl_heuristic"]
+    eng.close()
+
+
+def test_bad_queries_are_rejected_not_fatal(chunglu_small):
+    from scs_gb300.engine import BAD_QUERY, Engine
+    eng = Engine(graph=chunglu_small, limit_queries=4, stack_words=1 << 22, pool_words=1 << 24)
+    res = eng.solve([(3, 8, 10 ** 7, 1, 1), (9, 5, 10, 1, 1), (3, 600, 10, 1, 1)])
+    assert [r["status"] for r in res] == [BAD_QUERY] * 3
+    ok = eng.solve([(3, 6, 10, 1, 1)])[0]
+    assert ok["status"] in (0, 1)
+    eng.close()
