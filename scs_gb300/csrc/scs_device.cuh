@@ -193,7 +193,10 @@ struct SearchParams {
 };
 
 constexpr int PREP_THREADS = 512;
-constexpr int SEARCH_THREADS = 128;
+#ifndef SCS_SEARCH_THREADS
+#define SCS_SEARCH_THREADS 128
+#endif
+constexpr int SEARCH_THREADS = SCS_SEARCH_THREADS;
 
 __global__ void prep_kernel(DevGraph g, SlotArrays sa, Slot *slots,
                             const PrepJob *jobs, int njobs, PrepScratch ps,
