@@ -21,7 +21,7 @@ import time
 import numpy as np
 
 CACHE_DIR = os.environ.get("SCS_TUNE_DIR", os.path.join(os.path.expanduser("~"), ".cache", "scs_gb300"))
-DEFAULT_GRID = [(6, 20000), (4, 20000), (3, 20000), (2, 20000)]
+DEFAULT_GRID = [(3, 20000), (2, 20000)]
 
 
 def graph_key(off, adj, rows):

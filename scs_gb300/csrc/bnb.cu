@@ -1208,7 +1208,7 @@ __device__ void set_task_header(const SearchParams &P, Sh &sh,
 // test entry: one deterministic step per CTA, all children written in
 // canonical order Include, Dom_0..Dom_{k-1}, Exclude (dead ones skipped)
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(BT, 768 / BT)
+__global__ void __launch_bounds__(BT, SEARCH_MINB)
 step_test_kernel(SearchParams P) {
   extern __shared__ uint32_t dyn[];
   __shared__ Sh sh;
@@ -1390,7 +1390,7 @@ __device__ void stack_make_room(const SearchParams &P, uint32_t *sbase,
   __syncthreads();
 }
 
-__global__ void __launch_bounds__(BT, 768 / BT)
+__global__ void __launch_bounds__(BT, SEARCH_MINB)
 search_kernel(SearchParams P) {
   extern __shared__ uint32_t dyn[];
   __shared__ Sh sh;

@@ -187,9 +187,14 @@ static int engine_init(scs_engine *E) {
   // search grid and shared memory
   int max_optin = 0;
   CK(cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, E->dev));
-  // CTAs per SM: several small CTAs keep several tasks in flight per SM so
-  // one task's serial phases overlap with the others' work
-  uint32_t cps = c.ctas_per_sm ? c.ctas_per_sm : 6;
+  // CTAs per SM: several CTAs keep several tasks in flight per SM so one
+  // task's serial phases overlap with the others' work.  The default is as
+  // many as the kernel's registers allow; the shared memory left per CTA
+  // then decides how many state words stay on chip.
+  int occ_regs = 0;
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_regs, search_kernel, SEARCH_THREADS, 0));
+  uint32_t cps = c.ctas_per_sm ? c.ctas_per_sm : (uint32_t)SEARCH_MINB;
+  if (occ_regs >= 1) cps = std::min<uint32_t>(cps, (uint32_t)occ_regs);
   size_t stat = search_static_smem();
   size_t per_sm = 228 * 1024;
   size_t budget = std::min((size_t)max_optin, per_sm / cps - 1024);

@@ -193,10 +193,16 @@ struct SearchParams {
 };
 
 constexpr int PREP_THREADS = 512;
+// Search CTA shape: 256 threads, registers sized for 3 resident CTAs per SM
+// (measured fastest of 128/256/384/512 threads on the R-MAT scale-15 queries)
 #ifndef SCS_SEARCH_THREADS
-#define SCS_SEARCH_THREADS 128
+#define SCS_SEARCH_THREADS 256
+#endif
+#ifndef SCS_SEARCH_MINB
+#define SCS_SEARCH_MINB 3
 #endif
 constexpr int SEARCH_THREADS = SCS_SEARCH_THREADS;
+constexpr int SEARCH_MINB = SCS_SEARCH_MINB;
 
 __global__ void prep_kernel(DevGraph g, SlotArrays sa, Slot *slots,
                             const PrepJob *jobs, int njobs, PrepScratch ps,
