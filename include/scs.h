@@ -147,7 +147,8 @@ int scs_stats(scs_engine *e, uint64_t *out);
  * over CTAs [0 load, 1 min degree + rule 3, 2 rules 1/2, 3 bounds, 4 ustar,
  * 5 doms, 6 children, 7 other], then rule-1/2 rounds, rule-3 rounds, steps,
  * rule-1/2 cycles in [check passes, removal scans, compaction], removed
- * vertices and the row words their removal scanned. */
+ * vertices and the row words their removal scanned.  The last five are zero
+ * unless the library was built with -DSCS_PROF_MODE=1. */
 int scs_profile(scs_engine *e, uint64_t *out);
 
 /* Text of the last error on this engine (or the last creation failure). */

@@ -31,7 +31,7 @@ constexpr int BT = SEARCH_THREADS;
 #define SCS_R12_BALANCED 0
 #endif
 #ifndef SCS_MASK_SCORES
-#define SCS_MASK_SCORES 0
+#define SCS_MASK_SCORES 1
 #endif
 #ifndef SCS_R12_RECOUNT
 #define SCS_R12_RECOUNT 1
@@ -40,6 +40,20 @@ constexpr int BT = SEARCH_THREADS;
 #define SCS_ROW_UNROLL 8
 #endif
 constexpr int NWARP = BT / 32;
+
+// What the four sub-phase counters of scs_profile measure (they cost a few
+// per cent, so the default build leaves them at zero):
+// 0 nothing,
+// 1 rule-1/2 sub-phases (check passes, removal scans, compaction; removed
+//   vertices and their row words),
+// 2 step cycles by task size at entry (s < 512, s < 4096, larger; step
+//   counts of the first two buckets),
+// 3 ustar sub-phases (candidate collection, score push, argmax; summed |C|
+//   and candidate counts).
+#ifndef SCS_PROF_MODE
+#define SCS_PROF_MODE 0
+#endif
+constexpr bool PROF_R12 = SCS_PROF_MODE == 1;
 
 struct Sh {
   uint32_t slot, s, csize, n_local, l, h, ldoms, rules, kl, q_local, dmax;
@@ -295,6 +309,51 @@ __device__ __forceinline__ void warp_row_scan(const Task &T, uint32_t x, F f) {
   }
 }
 
+// Row scans that update memory: pred(nb) is evaluated for all of a thread's
+// SCS_ROW_UNROLL neighbours before any apply(nb) runs.  The compiler cannot
+// tell that apply's stores miss the next neighbours' state words, so with
+// one combined lambda each load waited for the previous update; rows are
+// strictly ascending (no repeated neighbour), so hoisting the loads is exact.
+template <class P, class A>
+__device__ __forceinline__ void warp_row_update(const Task &T, uint32_t x, P pred, A apply) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t b = T.off[x], e = T.off[x + 1];
+  for (uint32_t k0 = b; k0 < e; k0 += 32 * SCS_ROW_UNROLL) {
+    uint32_t nb[SCS_ROW_UNROLL];
+    bool ok[SCS_ROW_UNROLL];
+#pragma unroll
+    for (int j = 0; j < SCS_ROW_UNROLL; j++) {
+      uint32_t k = k0 + 32 * j + lane;
+      nb[j] = k < e ? T.adj[k] : SENT;
+    }
+#pragma unroll
+    for (int j = 0; j < SCS_ROW_UNROLL; j++) ok[j] = nb[j] != SENT && pred(nb[j]);
+#pragma unroll
+    for (int j = 0; j < SCS_ROW_UNROLL; j++)
+      if (ok[j]) apply(nb[j]);
+  }
+}
+
+template <class P, class A>
+__device__ __forceinline__ void block_row_update(const Task &T, uint32_t x, P pred, A apply) {
+  const int t = threadIdx.x;
+  const uint32_t b = T.off[x], e = T.off[x + 1];
+  for (uint32_t k0 = b; k0 < e; k0 += BT * SCS_ROW_UNROLL) {
+    uint32_t nb[SCS_ROW_UNROLL];
+    bool ok[SCS_ROW_UNROLL];
+#pragma unroll
+    for (int j = 0; j < SCS_ROW_UNROLL; j++) {
+      uint32_t k = k0 + BT * j + t;
+      nb[j] = k < e ? T.adj[k] : SENT;
+    }
+#pragma unroll
+    for (int j = 0; j < SCS_ROW_UNROLL; j++) ok[j] = nb[j] != SENT && pred(nb[j]);
+#pragma unroll
+    for (int j = 0; j < SCS_ROW_UNROLL; j++)
+      if (ok[j]) apply(nb[j]);
+  }
+}
+
 // Block-wide scan of one padded row (all threads), SCS_ROW_UNROLL loads in
 // flight per thread.
 template <class F>
@@ -542,13 +601,15 @@ __device__ void rule12(Task &T, Sh &sh, bool test) {
       }
       __syncthreads();
       const uint32_t nr = sh.cnt[1];
-      if (t == 0) sh.sub[0] += clock64() - c0;
+      if (PROF_R12 && t == 0) sh.sub[0] += clock64() - c0;
       if (nr == 0) break;
       c0 = clock64();
       if (t == 0) {
         sh.r12++;
-        sh.cnt4[0] += nr;
-        sh.cnt4[2] += s - nr;
+        if (PROF_R12) {
+          sh.cnt4[0] += nr;
+          sh.cnt4[2] += s - nr;
+        }
       }
       removed += nr;
       for (uint32_t i = t; i < nr; i += BT) T.W[T.tmp[i]] = ST_X << 30;
@@ -566,7 +627,7 @@ __device__ void rule12(Task &T, Sh &sh, bool test) {
           if (lane == 0) T.W[y] = (wy & ~DMASK) | c;
         }
         __syncthreads();
-        if (t == 0) sh.sub[1] += clock64() - c0;
+        if (PROF_R12 && t == 0) sh.sub[1] += clock64() - c0;
         continue;
       }
       // neighbours lose one R neighbour each (non-returning reductions)
@@ -577,14 +638,14 @@ __device__ void rule12(Task &T, Sh &sh, bool test) {
 #else
       for (uint32_t ri = wid; ri < nr; ri += NWARP) {
         uint32_t x = T.tmp[ri];
-        if (lane == 0) atomicAdd(&sh.cnt4[1], (unsigned long long)(T.off[x + 1] - T.off[x]));
-        warp_row_scan(T, x, [&](uint32_t nb) {
-          if (live(T.W[nb])) atomicSub(&T.W[nb], 1u);
-        });
+        if (PROF_R12 && lane == 0)
+          atomicAdd(&sh.cnt4[1], (unsigned long long)(T.off[x + 1] - T.off[x]));
+        warp_row_update(T, x, [&](uint32_t nb) { return live(T.W[nb]); },
+                        [&](uint32_t nb) { atomicSub(&T.W[nb], 1u); });
       }
       __syncthreads();
 #endif
-      if (t == 0) sh.sub[1] += clock64() - c0;
+      if (PROF_R12 && t == 0) sh.sub[1] += clock64() - c0;
     }
   }
   unsigned long long c1 = clock64();
@@ -600,7 +661,7 @@ __device__ void rule12(Task &T, Sh &sh, bool test) {
   }
   if (t == 0) {
     sh.nR = sh.s - sh.csize;
-    sh.sub[2] += clock64() - c1;
+    if (PROF_R12) sh.sub[2] += clock64() - c1;
   }
   __syncthreads();
 }
@@ -693,7 +754,9 @@ __device__ void bounds(Task &T, Sh &sh) {
 // dC(u) == 0 happens only for |C| == 1 (the root), where that partial sum is
 // 0 and ssc is not used for it.
 // ---------------------------------------------------------------------------
-__device__ void score_candidates(Task &T, Sh &sh) {
+// Returns true when ssc holds C-neighbour masks (summed by choose_ustar)
+// instead of scores.
+__device__ bool score_candidates(Task &T, Sh &sh) {
   const int t = threadIdx.x;
   const uint32_t cs = min(sh.csize, (uint32_t)CL_CAP);
   // C in ascending id order (rank sort into sh.A)
@@ -704,31 +767,66 @@ __device__ void score_candidates(Task &T, Sh &sh) {
   }
   __syncthreads();
   if (SCS_MASK_SCORES && cs <= 64) {
-    // every C row at once: candidate v collects a mask of its C neighbours
-    // (bit r = r-th smallest C id); one thread per candidate then sums the
-    // terms in bit order = ascending neighbour order, as the oracle does
+    // Every C row at once: candidate v collects a mask of its C neighbours
+    // (bit r = r-th smallest C id) with non-returning atomics; the argmax
+    // pass then sums the terms in bit order, which is ascending neighbour
+    // order, as the oracle does.  The rows are cut into chunks of one warp's
+    // SCS_ROW_UNROLL x 32 entries and the warps take chunks round-robin, so
+    // one barrier covers all of C.
+    constexpr uint32_t CH = 32 * SCS_ROW_UNROLL;
+    const int lane = t & 31, wid = t >> 5;
     for (uint32_t r = t; r < cs; r += BT) {
-      uint32_t dc = dc_of(T.W[sh.A[r]]);
+      const uint32_t u = sh.A[r];
+      const uint32_t dc = dc_of(T.W[u]);
       sh.wtab[r] = dc ? __ddiv_rn(1.0, (double)dc) : 1.0;
-    }
-    unsigned long long *mask = reinterpret_cast<unsigned long long *>(T.ssc);
-    for_rows_balanced(T, sh, sh.A, cs, T.tmp + sh.stride, [&](uint32_t r, uint32_t nb) {
-      if (st_of(T.W[nb]) == ST_R) atomicOr(&mask[nb], 1ull << r);
-    });
-    const uint32_t nc = sh.cnt[0];
-    for (uint32_t ci = t; ci < nc; ci += BT) {
-      uint32_t x = T.tmp[ci];
-      unsigned long long m = mask[x];
-      double sc = 0.0;
-      while (m) {
-        int r = __ffsll((long long)m) - 1;
-        m &= m - 1;
-        sc = __dadd_rn(sc, sh.wtab[r]);
-      }
-      T.ssc[x] = sc;  // the mask word becomes the score
+      const uint32_t b = T.off[u], e = T.off[u + 1];
+      sh.hist[r] = b;
+      sh.hist[64 + r] = e;
+      sh.B[r] = (e - b + CH - 1) / CH;
     }
     __syncthreads();
-    return;
+    if (wid == 0) {  // exclusive prefix of the chunk counts, two per lane
+      const uint32_t a = 2 * lane < cs ? sh.B[2 * lane] : 0;
+      const uint32_t c = 2 * lane + 1 < cs ? sh.B[2 * lane + 1] : 0;
+      uint32_t x = a + c;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+      }
+      const uint32_t ex = x - a - c;
+      __syncwarp();
+      if (2 * lane < cs) sh.B[2 * lane] = ex;
+      if (2 * lane + 1 < cs) sh.B[2 * lane + 1] = ex + a;
+      if (lane == 31) sh.B[64] = x;
+    }
+    __syncthreads();
+    const uint32_t total = sh.B[64];
+    unsigned long long *mask = reinterpret_cast<unsigned long long *>(T.ssc);
+    for (uint32_t c = wid; c < total; c += NWARP) {
+      uint32_t lo = 0, hi = cs;  // row of chunk c: last r with B[r] <= c
+      while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (sh.B[mid] <= c) lo = mid;
+        else hi = mid;
+      }
+      const uint32_t k0 = sh.hist[lo] + (c - sh.B[lo]) * CH, e = sh.hist[64 + lo];
+      uint32_t nb[SCS_ROW_UNROLL];
+      bool ok[SCS_ROW_UNROLL];
+#pragma unroll
+      for (int j = 0; j < SCS_ROW_UNROLL; j++) {
+        const uint32_t k = k0 + 32 * j + lane;
+        nb[j] = k < e ? T.adj[k] : SENT;
+      }
+#pragma unroll
+      for (int j = 0; j < SCS_ROW_UNROLL; j++)
+        ok[j] = nb[j] != SENT && st_of(T.W[nb[j]]) == ST_R;
+#pragma unroll
+      for (int j = 0; j < SCS_ROW_UNROLL; j++)
+        if (ok[j]) atomicOr(&mask[nb[j]], 1ull << lo);
+    }
+    __syncthreads();
+    return true;
   }
   for (uint32_t ci = 0; ci < cs; ci++) {
     const uint32_t u = sh.A[ci];
@@ -742,18 +840,28 @@ __device__ void score_candidates(Task &T, Sh &sh) {
         uint32_t k = k0 + BT * j + t;
         nb[j] = k < e ? T.adj[k] : SENT;
       }
+      // all state words, then all scores, then the stores: the neighbours of
+      // one row are distinct, so the loads need not wait for earlier stores
+      bool ok[SCS_ROW_UNROLL];
+      double sv[SCS_ROW_UNROLL];
 #pragma unroll
       for (int j = 0; j < SCS_ROW_UNROLL; j++)
-        if (nb[j] != SENT && st_of(T.W[nb[j]]) == ST_R)
-          T.ssc[nb[j]] = __dadd_rn(T.ssc[nb[j]], wu);
+        ok[j] = nb[j] != SENT && st_of(T.W[nb[j]]) == ST_R;
+#pragma unroll
+      for (int j = 0; j < SCS_ROW_UNROLL; j++) sv[j] = ok[j] ? T.ssc[nb[j]] : 0.0;
+#pragma unroll
+      for (int j = 0; j < SCS_ROW_UNROLL; j++)
+        if (ok[j]) T.ssc[nb[j]] = __dadd_rn(sv[j], wu);
     }
     __syncthreads();
   }
+  return false;
 }
 
 __device__ void choose_ustar(Task &T, Sh &sh) {
   const int t = threadIdx.x;
   const uint32_t s = sh.s;
+  unsigned long long c0 = SCS_PROF_MODE == 3 ? clock64() : 0;
   if (t == 0) sh.cnt[0] = 0;
   __syncthreads();
   for (uint32_t i0 = 0; i0 < s; i0 += BT) {
@@ -769,13 +877,37 @@ __device__ void choose_ustar(Task &T, Sh &sh) {
   }
   __syncthreads();
   const uint32_t nc = sh.cnt[0];
-  score_candidates(T, sh);
+  if (SCS_PROF_MODE == 3 && t == 0) {
+    const unsigned long long c1 = clock64();
+    sh.sub[0] += c1 - c0;
+    c0 = c1;
+    sh.cnt4[0] += min(sh.csize, (uint32_t)CL_CAP);
+    sh.cnt4[1] += nc;
+  }
+  const bool masked = score_candidates(T, sh);
+  if (SCS_PROF_MODE == 3 && t == 0) {
+    const unsigned long long c1 = clock64();
+    sh.sub[1] += c1 - c0;
+    c0 = c1;
+  }
   const double dmax = (double)sh.dmax;
   double best = 0.0;
   uint32_t bid = UINT32_MAX;
   for (uint32_t ci = t; ci < nc; ci += BT) {
     uint32_t x = T.tmp[ci];
-    double sc = T.ssc[x];
+    double sc;
+    if (masked) {
+      unsigned long long m = reinterpret_cast<const unsigned long long *>(T.ssc)[x];
+      sc = 0.0;
+      while (m) {
+        const int r = __ffsll((long long)m) - 1;
+        m &= m - 1;
+        sc = __dadd_rn(sc, sh.wtab[r]);
+      }
+      T.ssc[x] = sc;  // the mask word becomes the pushed score
+    } else {
+      sc = T.ssc[x];
+    }
     if (sc > 0.0) sc = __dadd_rn(sc, __ddiv_rn((double)dr_of(T.W[x]), dmax));
     if (sc > best || (sc == best && sc > 0.0 && x < bid)) {
       best = sc;
@@ -788,6 +920,7 @@ __device__ void choose_ustar(Task &T, Sh &sh) {
   if (t == 0) {
     sh.ustar = (osc > 0.0) ? oid : UINT32_MAX;
     sh.ndom_cand = nc;
+    if (SCS_PROF_MODE == 3) sh.sub[2] += clock64() - c0;
   }
   __syncthreads();
 }
@@ -821,9 +954,8 @@ __device__ void find_doms(Task &T, Sh &sh) {
   const uint32_t wu = T.W[u];
   const uint32_t degu = dc_of(wu) + dr_of(wu), dcu = dc_of(wu);
   // mark N_T(u*) and u*
-  block_row_scan(T, u, [&](uint32_t nb) {
-    if (live(T.W[nb])) T.aux[nb] = 1u;
-  });
+  block_row_update(T, u, [&](uint32_t nb) { return live(T.W[nb]); },
+                   [&](uint32_t nb) { T.aux[nb] = 1u; });
   if (t == 0) T.aux[u] = 1u;
   __syncthreads();
   // candidates (R, dC > 0) are in tmp[0..nc); necessary conditions for
@@ -939,9 +1071,8 @@ __device__ void mark_children(Task &T, Sh &sh) {
   // adjacency bits: warp per marked vertex
   for (uint32_t j = wid; j <= k; j += NWARP) {
     uint32_t v = j == 0 ? sh.ustar : sh.doms[j - 1];
-    warp_row_scan(T, v, [&](uint32_t nb) {
-      if (live(T.W[nb])) atomicOr(&T.aux[nb], 1u << j);
-    });
+    warp_row_update(T, v, [&](uint32_t nb) { return live(T.W[nb]); },
+                    [&](uint32_t nb) { atomicOr(&T.aux[nb], 1u << j); });
   }
   __syncthreads();
   if (t == 0) {
@@ -1507,7 +1638,18 @@ search_kernel(SearchParams P) {
       clear_state(T, sh);
       continue;
     }
+#if SCS_PROF_MODE == 2
+    const uint32_t s_in = sh.s;
+    const unsigned long long c_step = clock64();
+#endif
     step_core(T, sh, false, nullptr);
+#if SCS_PROF_MODE == 2
+    if (t == 0) {
+      const int b = s_in < 512 ? 0 : s_in < 4096 ? 1 : 2;
+      sh.sub[b] += clock64() - c_step;
+      if (b < 2) sh.cnt4[b]++;
+    }
+#endif
     local_nodes++;
     uint32_t pushed = 0;
     bool cont = false;
