@@ -36,6 +36,11 @@ constexpr int BT = SEARCH_THREADS;
 #ifndef SCS_R12_RECOUNT
 #define SCS_R12_RECOUNT 1
 #endif
+// rows of at most this many words (padding included) are scanned by one
+// thread in rule-1/2 removals and recounts; longer rows by a warp
+#ifndef SCS_LANE_ROW
+#define SCS_LANE_ROW 128
+#endif
 #ifndef SCS_ROW_UNROLL
 #define SCS_ROW_UNROLL 8
 #endif
@@ -49,7 +54,9 @@ constexpr int NWARP = BT / 32;
 // 2 step cycles by task size at entry (s < 512, s < 4096, larger; step
 //   counts of the first two buckets),
 // 3 ustar sub-phases (candidate collection, score push, argmax; summed |C|
-//   and candidate counts).
+//   and candidate counts),
+// 4 as 0, but the phase cycles count only steps on tasks of fewer than 512
+//   entries.
 #ifndef SCS_PROF_MODE
 #define SCS_PROF_MODE 0
 #endif
@@ -75,6 +82,7 @@ struct Sh {
   unsigned long long cnt4[4];  // removed vertices, removed row words, survivors, -
   float mean_deg;            // local CSR entries per local vertex (this query)
   int have;
+  int prof_small;  // profile mode 4: this step's task has < 512 entries
   int stop;
   unsigned long long rec;
   uint32_t red_u[NWARP];
@@ -187,7 +195,7 @@ __device__ __forceinline__ void phase_mark(Sh &sh, int which) {
   // thread 0 only: charge the cycles since the last mark to phase `which`
   if (threadIdx.x == 0) {
     unsigned long long now = clock64();
-    sh.ph[which] += now - sh.t_ph;
+    if (SCS_PROF_MODE != 4 || sh.prof_small) sh.ph[which] += now - sh.t_ph;
     sh.t_ph = now;
   }
 }
@@ -351,6 +359,26 @@ __device__ __forceinline__ void block_row_update(const Task &T, uint32_t x, P pr
 #pragma unroll
     for (int j = 0; j < SCS_ROW_UNROLL; j++)
       if (ok[j]) apply(nb[j]);
+  }
+}
+
+// One thread walks a short padded row [b, e) with 16-byte loads (rows start
+// 16-byte aligned and are padded to 4 words), 8 words per iteration; pred
+// runs on all 8 before apply, as in warp_row_update.
+template <class P, class A>
+__device__ __forceinline__ void lane_row_update(const Task &T, uint32_t b, uint32_t e,
+                                                P pred, A apply) {
+  for (uint32_t k = b; k < e; k += 8) {
+    const uint4 q4 = *reinterpret_cast<const uint4 *>(T.adj + k);
+    const uint4 r4 = k + 4 < e ? *reinterpret_cast<const uint4 *>(T.adj + k + 4)
+                               : make_uint4(SENT, SENT, SENT, SENT);
+    const uint32_t nb8[8] = {q4.x, q4.y, q4.z, q4.w, r4.x, r4.y, r4.z, r4.w};
+    bool ok[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) ok[j] = nb8[j] != SENT && pred(nb8[j]);
+#pragma unroll
+    for (int j = 0; j < 8; j++)
+      if (ok[j]) apply(nb8[j]);
   }
 }
 
@@ -586,7 +614,10 @@ __device__ void rule12(Task &T, Sh &sh, bool test) {
       const uint32_t kl = sh.kl, cs = sh.csize, s = sh.s;
       const uint32_t ubd = ubd_dev(kl, h);
       unsigned long long c0 = clock64();
-      if (t == 0) sh.cnt[1] = 0;
+      if (t == 0) {
+        sh.cnt[1] = 0;
+        sh.cnt[2] = 0;  // long rows of this round's removals / recounts
+      }
       __syncthreads();
       for (uint32_t i0 = 0; i0 < s; i0 += BT) {
         uint32_t i = i0 + t;
@@ -617,10 +648,35 @@ __device__ void rule12(Task &T, Sh &sh, bool test) {
       if (SCS_R12_RECOUNT && s - nr < nr) {
         // burst: fewer survivors than removals -- recount each survivor's R
         // neighbours (exact, cost sum deg(survivors) < sum deg(removed))
-        for (uint32_t i = wid; i < s; i += NWARP) {
-          const uint32_t y = T.list[i];
+        // Short rows one thread each, long rows a warp each.  Writing W[y]
+        // changes only y's dR bits; the other threads read status bits only.
+        uint32_t *longs = T.tmp + sh.stride;
+        for (uint32_t i0 = 0; i0 < s; i0 += BT) {
+          const uint32_t i = i0 + t;
+          bool lng = false;
+          uint32_t y = 0;
+          if (i < s) {
+            y = T.list[i];
+            const uint32_t wy = T.W[y];
+            if (live(wy)) {
+              const uint32_t b = T.off[y], e = T.off[y + 1];
+              if (e - b > SCS_LANE_ROW) {
+                lng = true;
+              } else {
+                uint32_t c = 0;
+                lane_row_update(T, b, e, [&](uint32_t nb) { return st_of(T.W[nb]) == ST_R; },
+                                [&](uint32_t) { c++; });
+                T.W[y] = (wy & ~DMASK) | c;
+              }
+            }
+          }
+          warp_append(lng, y, &sh.cnt[2], longs);
+        }
+        __syncthreads();
+        const uint32_t nl = sh.cnt[2];
+        for (uint32_t i = wid; i < nl; i += NWARP) {
+          const uint32_t y = longs[i];
           const uint32_t wy = T.W[y];
-          if (!live(wy)) continue;
           uint32_t c = 0;
           warp_row_scan(T, y, [&](uint32_t nb) { c += st_of(T.W[nb]) == ST_R; });
           c = warp_sum(c);
@@ -636,14 +692,32 @@ __device__ void rule12(Task &T, Sh &sh, bool test) {
         if (live(T.W[nb])) atomicSub(&T.W[nb], 1u);
       });
 #else
-      for (uint32_t ri = wid; ri < nr; ri += NWARP) {
-        uint32_t x = T.tmp[ri];
-        if (PROF_R12 && lane == 0)
-          atomicAdd(&sh.cnt4[1], (unsigned long long)(T.off[x + 1] - T.off[x]));
-        warp_row_update(T, x, [&](uint32_t nb) { return live(T.W[nb]); },
-                        [&](uint32_t nb) { atomicSub(&T.W[nb], 1u); });
+      {
+        // short rows one thread each (16-byte loads), long rows a warp each
+        uint32_t *longs = T.tmp + sh.stride;
+        for (uint32_t i0 = 0; i0 < nr; i0 += BT) {
+          const uint32_t i = i0 + t;
+          bool lng = false;
+          uint32_t x = 0;
+          if (i < nr) {
+            x = T.tmp[i];
+            const uint32_t b = T.off[x], e = T.off[x + 1];
+            if (PROF_R12) atomicAdd(&sh.cnt4[1], (unsigned long long)(e - b));
+            if (e - b > SCS_LANE_ROW)
+              lng = true;
+            else
+              lane_row_update(T, b, e, [&](uint32_t nb) { return live(T.W[nb]); },
+                              [&](uint32_t nb) { atomicSub(&T.W[nb], 1u); });
+          }
+          warp_append(lng, x, &sh.cnt[2], longs);
+        }
+        __syncthreads();
+        const uint32_t nl = sh.cnt[2];
+        for (uint32_t ri = wid; ri < nl; ri += NWARP)
+          warp_row_update(T, longs[ri], [&](uint32_t nb) { return live(T.W[nb]); },
+                          [&](uint32_t nb) { atomicSub(&T.W[nb], 1u); });
+        __syncthreads();
       }
-      __syncthreads();
 #endif
       if (PROF_R12 && t == 0) sh.sub[1] += clock64() - c0;
     }
@@ -1548,6 +1622,7 @@ search_kernel(SearchParams P) {
     for (int i = 0; i < 8; i++) sh.ph[i] = 0;
     for (int i = 0; i < 4; i++) sh.sub[i] = sh.cnt4[i] = 0;
     sh.r12 = sh.r3 = 0;
+    sh.prof_small = 0;
     sh.t_ph = clock64();
   }
   __syncthreads();
@@ -1638,6 +1713,9 @@ search_kernel(SearchParams P) {
       clear_state(T, sh);
       continue;
     }
+#if SCS_PROF_MODE == 4
+    if (t == 0) sh.prof_small = sh.s < 512;
+#endif
 #if SCS_PROF_MODE == 2
     const uint32_t s_in = sh.s;
     const unsigned long long c_step = clock64();
