@@ -36,6 +36,12 @@ constexpr int BT = SEARCH_THREADS;
 #ifndef SCS_R12_RECOUNT
 #define SCS_R12_RECOUNT 1
 #endif
+// dominance test: words of a candidate's row one thread checks before a warp
+// takes over the rest
+#ifndef SCS_LANE_DOM
+#define SCS_LANE_DOM 32
+#endif
+static_assert(SCS_LANE_DOM % 8 == 0, "stage 1 checks whole 8-word groups");
 // rows of at most this many words (padding included) are scanned by one
 // thread in rule-1/2 removals and recounts; longer rows by a warp
 #ifndef SCS_LANE_ROW
@@ -56,7 +62,10 @@ constexpr int NWARP = BT / 32;
 // 3 ustar sub-phases (candidate collection, score push, argmax; summed |C|
 //   and candidate counts),
 // 4 as 0, but the phase cycles count only steps on tasks of fewer than 512
-//   entries.
+//   entries,
+// 5 dominated-vertex sub-phases (marking N(u*) + test stage 1, test stage
+//   2, the rest up to the child marks; candidates passing the prefilters and
+//   candidates reaching stage 2).
 #ifndef SCS_PROF_MODE
 #define SCS_PROF_MODE 0
 #endif
@@ -70,6 +79,7 @@ struct Sh {
   uint32_t p1, p2, nR;
   uint32_t ustar, us_idx;
   uint32_t ndoms, ndom_cand;
+  uint32_t masked;  // this step's scores came from C-neighbour masks
   uint32_t doms[MAX_DOMS];
   uint32_t doms_idx[MAX_DOMS];
   uint32_t wit_pending;
@@ -211,7 +221,8 @@ struct Task {
   uint32_t *aux;
   uint32_t *tmp;
   double *ssc;   // pushed ustar scores, by local id (zero between uses)
-  double *dsc;   // pushed dom-score partial sums, by local id
+  unsigned long long *cmask;  // C-neighbour masks of the candidates, by local id
+  uint32_t *bits;  // N[u*] as a bitmap in shared memory after W (null: aux)
   double *dsc2;  // scores of dominated candidates, by position
   const uint32_t *off;
   const uint32_t *adj;
@@ -443,8 +454,8 @@ __device__ void eval_mindeg(Task &T, Sh &sh, bool test, uint32_t *t_wit) {
   if (md == UINT32_MAX) return;
   bool improve_step = (sh.best == UINT32_MAX || md > sh.best);
   if (improve_step && t == 0) sh.best = md;
-  if (md > sh.kl && t == 0) sh.kl = md;
   if (test) {
+    if (md > sh.kl && t == 0) sh.kl = md;
     if (improve_step) {
       for (uint32_t i = t; i < cs; i += BT) t_wit[i] = sh.cl[i];
       if (t == 0) t_wit[CL_CAP] = cs;  // count stored past the list
@@ -452,10 +463,16 @@ __device__ void eval_mindeg(Task &T, Sh &sh, bool test, uint32_t *t_wit) {
     __syncthreads();
     return;
   }
-  // global incumbent + witness (bounded lock)
+  // global incumbent + witness (bounded lock).  The slot's incumbent is never
+  // below sh.kl (sh.kl only takes values already in the slot), so unless md
+  // beats sh.kl the atomic cannot raise it.
   if (t == 0) {
-    uint32_t old = atomicMax(&T.slot->kl, md);
     sh.wit_pending = 0;
+    uint32_t old = UINT32_MAX;
+    if (md > sh.kl) {
+      sh.kl = md;
+      old = atomicMax(&T.slot->kl, md);
+    }
     if (old < md) {
       uint32_t spins = 0;
       while (atomicCAS(&T.slot->wit_lock, 0u, 1u) != 0u) {
@@ -947,7 +964,8 @@ __device__ void choose_ustar(Task &T, Sh &sh) {
       uint32_t w = T.W[x];
       c = st_of(w) == ST_R && dc_of(w) > 0;
     }
-    warp_append(c, x, &sh.cnt[0], T.tmp);
+    // candidates carry their list position: (i << 16) | x (both < 2^16)
+    warp_append(c, (i << 16) | x, &sh.cnt[0], T.tmp);
   }
   __syncthreads();
   const uint32_t nc = sh.cnt[0];
@@ -966,12 +984,13 @@ __device__ void choose_ustar(Task &T, Sh &sh) {
   }
   const double dmax = (double)sh.dmax;
   double best = 0.0;
-  uint32_t bid = UINT32_MAX;
+  uint32_t bid = UINT32_MAX, bpos = 0;
   for (uint32_t ci = t; ci < nc; ci += BT) {
-    uint32_t x = T.tmp[ci];
+    const uint32_t pk = T.tmp[ci], x = pk & 0xFFFFu;
     double sc;
     if (masked) {
       unsigned long long m = reinterpret_cast<const unsigned long long *>(T.ssc)[x];
+      T.cmask[x] = m;  // kept for the dominance prefilter
       sc = 0.0;
       while (m) {
         const int r = __ffsll((long long)m) - 1;
@@ -986,14 +1005,17 @@ __device__ void choose_ustar(Task &T, Sh &sh) {
     if (sc > best || (sc == best && sc > 0.0 && x < bid)) {
       best = sc;
       bid = x;
+      bpos = pk >> 16;
     }
   }
   double osc;
   uint32_t oid;
   block_argmax(best, bid, sh, osc, oid);
+  if (osc > 0.0 && bid == oid) sh.us_idx = bpos;  // the one thread holding u*
   if (t == 0) {
     sh.ustar = (osc > 0.0) ? oid : UINT32_MAX;
     sh.ndom_cand = nc;
+    sh.masked = masked;
     if (SCS_PROF_MODE == 3) sh.sub[2] += clock64() - c0;
   }
   __syncthreads();
@@ -1002,18 +1024,8 @@ __device__ void choose_ustar(Task &T, Sh &sh) {
 // reset the pushed scores (candidates are exactly the R vertices with C
 // neighbours, i.e. every vertex that received a term)
 __device__ void clear_scores(Task &T, Sh &sh) {
-  for (uint32_t ci = threadIdx.x; ci < sh.ndom_cand; ci += BT) T.ssc[T.tmp[ci]] = 0.0;
+  for (uint32_t ci = threadIdx.x; ci < sh.ndom_cand; ci += BT) T.ssc[T.tmp[ci] & 0xFFFFu] = 0.0;
   __syncthreads();
-}
-
-__device__ uint32_t list_index(const uint32_t *list, uint32_t s, uint32_t x) {
-  uint32_t lo = 0, hi = s;
-  while (lo < hi) {
-    uint32_t mid = (lo + hi) >> 1;
-    if (list[mid] < x) lo = mid + 1;
-    else hi = mid;
-  }
-  return lo;
 }
 
 __device__ void find_doms(Task &T, Sh &sh) {
@@ -1022,15 +1034,23 @@ __device__ void find_doms(Task &T, Sh &sh) {
   if (t == 0) {
     sh.ndoms = 0;
     sh.cnt[1] = 0;
+    sh.cnt[2] = 0;
   }
   __syncthreads();
   if (sh.ldoms == 0) return;
   const uint32_t wu = T.W[u];
   const uint32_t degu = dc_of(wu) + dr_of(wu), dcu = dc_of(wu);
   // mark N_T(u*) and u*
-  block_row_update(T, u, [&](uint32_t nb) { return live(T.W[nb]); },
-                   [&](uint32_t nb) { T.aux[nb] = 1u; });
-  if (t == 0) T.aux[u] = 1u;
+  uint32_t *bits = T.bits;
+  auto mark = [&](uint32_t nb) {
+    if (bits) atomicOr(&bits[nb >> 5], 1u << (nb & 31));
+    else T.aux[nb] = 1u;
+  };
+  auto marked = [&](uint32_t nb) -> bool {
+    return bits ? (bits[nb >> 5] >> (nb & 31)) & 1u : T.aux[nb] != 0u;
+  };
+  block_row_update(T, u, [&](uint32_t nb) { return live(T.W[nb]); }, mark);
+  if (t == 0) mark(u);
   __syncthreads();
   // candidates (R, dC > 0) are in tmp[0..nc); necessary conditions for
   // N_T(v) within N_T(u*)+u*: dC(v) <= dC(u*), deg_T(v) <= deg_T(u*) + 1.
@@ -1040,49 +1060,112 @@ __device__ void find_doms(Task &T, Sh &sh) {
   const double dmax = (double)sh.dmax;
   const bool root_c = sh.csize <= 1;  // dom partial sum is 0 when |C| == 1
   uint32_t *dom_id = T.tmp + sh.s;  // second half of tmp (s <= n)
-  for (uint32_t ci = t; ci < nc; ci += BT) {
-    uint32_t x = T.tmp[ci];
-    if (x == u) continue;
-    uint32_t wx = T.W[x];
-    if (dc_of(wx) > dcu || dc_of(wx) + dr_of(wx) > degu + 1u) continue;
-    bool dom = true;
-    const uint32_t b = T.off[x], e = T.off[x + 1];
-    for (uint32_t k = b; k < e && dom; k += 8) {
-      const uint4 q4 = *reinterpret_cast<const uint4 *>(T.adj + k);
-      const uint4 r4 = k + 4 < e ? *reinterpret_cast<const uint4 *>(T.adj + k + 4)
-                                 : make_uint4(SENT, SENT, SENT, SENT);
-      const uint32_t nb8[8] = {q4.x, q4.y, q4.z, q4.w, r4.x, r4.y, r4.z, r4.w};
+  // With masks: v's C neighbours must all be neighbours of u* (u* is in R),
+  // so mask(v) within mask(u*) is necessary as well.
+  const bool use_mask = sh.masked;
+  const unsigned long long mu = use_mask ? T.cmask[u] : 0ull;
+  auto record = [&](uint32_t pk) {
+    const uint32_t x = pk & 0xFFFFu;
+    const double part = root_c ? 0.0 : T.ssc[x];
+    const double sc = __dadd_rn(part, __ddiv_rn((double)dr_of(T.W[x]), dmax));
+    const uint32_t k = atomicAdd(&sh.cnt[1], 1u);
+    dom_id[k] = pk;  // packed with the list position
+    T.dsc2[k] = sc;
+  };
+  // Stage 1, one thread per candidate: the prefilters and the first
+  // SCS_LANE_DOM words of the row, where most candidates fail.  Candidates
+  // still undecided go to a list (list2 is free here) for stage 2.
+  uint32_t *undec = T.list2;
+  for (uint32_t i0 = 0; i0 < nc; i0 += BT) {
+    const uint32_t ci = i0 + t;
+    bool more = false;
+    uint32_t pk = 0;
+    if (ci < nc) {
+      pk = T.tmp[ci];
+      const uint32_t x = pk & 0xFFFFu;
+      const uint32_t wx = T.W[x];
+      bool dom = x != u && dc_of(wx) <= dcu && dc_of(wx) + dr_of(wx) <= degu + 1u &&
+                 !(use_mask && (T.cmask[x] & ~mu));
+      if (dom) {
+        if (SCS_PROF_MODE == 5) atomicAdd(&sh.cnt4[0], 1ull);
+        const uint32_t b = T.off[x], e = T.off[x + 1];
+        const uint32_t stop = min(e, b + SCS_LANE_DOM);
+        for (uint32_t k = b; k < stop && dom; k += 8) {
+          const uint4 q4 = *reinterpret_cast<const uint4 *>(T.adj + k);
+          const uint4 r4 = k + 4 < e ? *reinterpret_cast<const uint4 *>(T.adj + k + 4)
+                                     : make_uint4(SENT, SENT, SENT, SENT);
+          const uint32_t nb8[8] = {q4.x, q4.y, q4.z, q4.w, r4.x, r4.y, r4.z, r4.w};
 #pragma unroll
-      for (int j = 0; j < 8; j++) {
-        uint32_t nb = nb8[j];
-        if (nb != SENT && live(T.W[nb]) && T.aux[nb] == 0u) dom = false;
+          for (int j = 0; j < 8; j++) {
+            const uint32_t nb = nb8[j];
+            if (nb != SENT && live(T.W[nb]) && !marked(nb)) dom = false;
+          }
+        }
+        if (dom) {
+          if (stop < e) more = true;
+          else record(pk);
+        }
       }
     }
-    if (dom) {
-      double part = root_c ? 0.0 : T.ssc[x];
-      double sc = __dadd_rn(part, __ddiv_rn((double)dr_of(wx), dmax));
-      uint32_t k = atomicAdd(&sh.cnt[1], 1u);
-      dom_id[k] = x;
-      T.dsc2[k] = sc;
+    warp_append(more, pk, &sh.cnt[2], undec);
+  }
+  __syncthreads();
+#if SCS_PROF_MODE == 5
+  unsigned long long c5 = clock64();
+  if (t == 0) {
+    sh.sub[0] += c5 - sh.t_ph;
+    sh.cnt4[1] += sh.cnt[2];
+  }
+#endif
+  // Stage 2, one warp per undecided candidate over the rest of its row.
+  {
+    const int lane = t & 31, wid = t >> 5;
+    const uint32_t nu = sh.cnt[2];
+    for (uint32_t j = wid; j < nu; j += NWARP) {
+      const uint32_t pk = undec[j], x = pk & 0xFFFFu;
+      const uint32_t e = T.off[x + 1];
+      bool dom = true;
+      for (uint32_t k0 = T.off[x] + SCS_LANE_DOM; k0 < e && dom; k0 += 32 * SCS_ROW_UNROLL) {
+        uint32_t nb[SCS_ROW_UNROLL];
+#pragma unroll
+        for (int q = 0; q < SCS_ROW_UNROLL; q++) {
+          const uint32_t k = k0 + 32 * q + lane;
+          nb[q] = k < e ? T.adj[k] : SENT;
+        }
+        bool bad = false;
+#pragma unroll
+        for (int q = 0; q < SCS_ROW_UNROLL; q++)
+          bad |= nb[q] != SENT && live(T.W[nb[q]]) && !marked(nb[q]);
+        dom = !__any_sync(0xffffffffu, bad);
+      }
+      if (dom && lane == 0) record(pk);
     }
   }
   __syncthreads();
+#if SCS_PROF_MODE == 5
+  if (t == 0) sh.sub[1] += clock64() - c5;
+#endif
   // clear marks
-  block_row_scan(T, u, [&](uint32_t nb) { T.aux[nb] = 0u; });
-  if (t == 0) T.aux[u] = 0u;
+  if (bits) {
+    for (uint32_t i = t; i < (sh.n_local + 31) / 32; i += BT) bits[i] = 0;
+  } else {
+    block_row_scan(T, u, [&](uint32_t nb) { T.aux[nb] = 0u; });
+    if (t == 0) T.aux[u] = 0u;
+  }
   __syncthreads();
   const uint32_t nd = sh.cnt[1];
   const uint32_t k = min(nd, min(sh.ldoms, (uint32_t)MAX_DOMS));
   for (uint32_t r = 0; r < k; r++) {
     double bs = -1.0;
-    uint32_t bi = UINT32_MAX, bpos = UINT32_MAX;
+    uint32_t bi = UINT32_MAX, bpos = UINT32_MAX, bli = 0;
     for (uint32_t i = t; i < nd; i += BT) {
       double sc = T.dsc2[i];
-      uint32_t x = dom_id[i];
+      const uint32_t pk = dom_id[i], x = pk & 0xFFFFu;
       if (sc > bs || (sc == bs && x < bi)) {
         bs = sc;
         bi = x;
         bpos = i;
+        bli = pk >> 16;
       }
     }
     double osc;
@@ -1091,6 +1174,7 @@ __device__ void find_doms(Task &T, Sh &sh) {
     if (bi == oid && bpos != UINT32_MAX && bs == osc) {
       T.dsc2[bpos] = -2.0;  // exclude from later rounds
       sh.doms[r] = oid;
+      sh.doms_idx[r] = bli;
     }
     __syncthreads();
   }
@@ -1149,14 +1233,10 @@ __device__ void mark_children(Task &T, Sh &sh) {
                     [&](uint32_t nb) { atomicOr(&T.aux[nb], 1u << j); });
   }
   __syncthreads();
-  if (t == 0) {
-    atomicOr(&T.aux[sh.ustar], 1u << 21);
-    sh.us_idx = list_index(T.list, sh.s, sh.ustar);
-  }
-  if (t < k) {
-    atomicOr(&T.aux[sh.doms[t]], (t + 1u) << 16);
-    sh.doms_idx[t] = list_index(T.list, sh.s, sh.doms[t]);
-  }
+  // list positions of u* (us_idx) and the d_j (doms_idx) came with the
+  // candidates
+  if (t == 0) atomicOr(&T.aux[sh.ustar], 1u << 21);
+  if (t < k) atomicOr(&T.aux[sh.doms[t]], (t + 1u) << 16);
   __syncthreads();
 }
 
@@ -1357,9 +1437,16 @@ __device__ void step_core(Task &T, Sh &sh, bool test, uint32_t *t_wit) {
     __syncthreads();
     return;
   }
+#if SCS_PROF_MODE == 5
+  unsigned long long c5 = clock64();
+#endif
   find_doms(T, sh);
   clear_scores(T, sh);
   mark_children(T, sh);
+#if SCS_PROF_MODE == 5
+  // everything but the two test stages
+  if (t == 0) sh.sub[2] += clock64() - c5;
+#endif
   phase_mark(sh, 5);
 }
 
@@ -1369,13 +1456,16 @@ __device__ Task make_task(const SearchParams &P, Sh &sh, uint32_t *dyn,
   const uint32_t slot = sh.slot;
   const size_t st = P.scr.stride;
   T.W = (sh.n_local <= P.nw_smem) ? dyn : P.scr.word + (size_t)cta * st;
+  // the dominance test's marks go to a bitmap behind the state words when
+  // both fit (the dynamic region is all zero between tasks)
+  T.bits = (sh.n_local + (sh.n_local + 31) / 32 <= P.nw_smem) ? dyn + sh.n_local : nullptr;
   T.list = P.scr.list + (size_t)cta * 2 * st;
   T.list2 = T.list + st;
   T.aux = P.scr.aux + (size_t)cta * st;
   T.tmp = P.scr.tmp + (size_t)cta * 2 * st;
   T.ssc = P.scr.dsc + (size_t)cta * 3 * st;
-  T.dsc = T.ssc + st;
-  T.dsc2 = T.dsc + st;
+  T.cmask = reinterpret_cast<unsigned long long *>(T.ssc + st);
+  T.dsc2 = T.ssc + 2 * st;
   T.off = P.sa.loc_off + (size_t)slot * (P.sa.stride_n + 1);
   T.adj = P.sa.loc_adj + (size_t)slot * P.sa.cap_adj;
   T.dist = P.sa.loc_dist + (size_t)slot * P.sa.stride_n;
@@ -1431,7 +1521,8 @@ step_test_kernel(SearchParams P) {
   }
   __syncthreads();
   Task T = make_task(P, sh, dyn, ti);
-  for (uint32_t i = threadIdx.x; i < sh.n_local && T.W == dyn; i += BT) dyn[i] = 0;
+  // state words and the bitmap behind them start at zero
+  for (uint32_t i = threadIdx.x; i < P.nw_smem; i += BT) dyn[i] = 0;
   __syncthreads();
   load_record(rec, T, sh);
   uint32_t *wit = P.t_wit + (size_t)ti * P.t_wit_stride;
