@@ -36,6 +36,17 @@ constexpr int BT = SEARCH_THREADS;
 #ifndef SCS_R12_RECOUNT
 #define SCS_R12_RECOUNT 1
 #endif
+// list passes (rule-1/2 checks, ustar candidates): entries per thread whose
+// loads are issued together
+#ifndef SCS_LIST_UNROLL
+#define SCS_LIST_UNROLL 4
+#endif
+// rule-1/2 removals: rows cut into chunks of this many words, 32 rows per
+// warp batch (0: short rows per thread, long rows per warp)
+#ifndef SCS_CHUNK_WORDS
+#define SCS_CHUNK_WORDS 32
+#endif
+static_assert(SCS_CHUNK_WORDS % 4 == 0, "chunks are whole 16-byte groups");
 // dominance test: words of a candidate's row one thread checks before a warp
 // takes over the rest
 #ifndef SCS_LANE_DOM
@@ -393,6 +404,68 @@ __device__ __forceinline__ void lane_row_update(const Task &T, uint32_t b, uint3
   }
 }
 
+// The rows of ids[0..cnt), taken 32 at a time by each warp (one per lane),
+// cut into SCS_CHUNK_WORDS-word chunks that the warp's lanes share: a warp
+// prefix of the chunk counts and a 5-step shuffle search give each lane its
+// row, so every lane keeps SCS_CHUNK_WORDS / 4 16-byte loads in flight
+// whatever the row lengths.  pred runs on a chunk's words before apply.
+template <class P, class A>
+__device__ __forceinline__ void warp_rows_chunked(const Task &T, const uint32_t *ids,
+                                                  uint32_t cnt, P pred, A apply) {
+  constexpr uint32_t CW = SCS_CHUNK_WORDS > 0 ? SCS_CHUNK_WORDS : 16;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (uint32_t base = wid * 32; base < cnt; base += NWARP * 32) {
+    const uint32_t i = base + lane;
+    uint32_t b = 0, len = 0;
+    if (i < cnt) {
+      const uint32_t x = ids[i];
+      b = T.off[x];
+      len = T.off[x + 1] - b;
+    }
+    const uint32_t c = (len + CW - 1) / CW;
+    uint32_t incl = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    const uint32_t excl = incl - c;
+    for (uint32_t k0 = 0; k0 < total; k0 += 32) {
+      const uint32_t k = k0 + lane;
+      uint32_t r = 0;  // last lane whose first chunk is at or before k
+#pragma unroll
+      for (uint32_t step = 16; step; step >>= 1) {
+        const uint32_t e2 = __shfl_sync(0xffffffffu, excl, r + step);
+        if (e2 <= k) r += step;
+      }
+      const uint32_t rb = __shfl_sync(0xffffffffu, b, r);
+      const uint32_t rex = __shfl_sync(0xffffffffu, excl, r);
+      const uint32_t rlen = __shfl_sync(0xffffffffu, len, r);
+      if (k < total) {
+        const uint32_t start = rb + (k - rex) * CW, end = min(rb + rlen, start + CW);
+        uint32_t nb[CW];
+#pragma unroll
+        for (uint32_t q = 0; q < CW / 4; q++) {
+          const uint4 v = start + 4 * q < end
+                              ? *reinterpret_cast<const uint4 *>(T.adj + start + 4 * q)
+                              : make_uint4(SENT, SENT, SENT, SENT);
+          nb[4 * q] = v.x;
+          nb[4 * q + 1] = v.y;
+          nb[4 * q + 2] = v.z;
+          nb[4 * q + 3] = v.w;
+        }
+        bool ok[CW];
+#pragma unroll
+        for (uint32_t j = 0; j < CW; j++) ok[j] = nb[j] != SENT && pred(nb[j]);
+#pragma unroll
+        for (uint32_t j = 0; j < CW; j++)
+          if (ok[j]) apply(nb[j]);
+      }
+    }
+  }
+}
+
 // Block-wide scan of one padded row (all threads), SCS_ROW_UNROLL loads in
 // flight per thread.
 template <class F>
@@ -636,16 +709,25 @@ __device__ void rule12(Task &T, Sh &sh, bool test) {
         sh.cnt[2] = 0;  // long rows of this round's removals / recounts
       }
       __syncthreads();
-      for (uint32_t i0 = 0; i0 < s; i0 += BT) {
-        uint32_t i = i0 + t;
-        bool rm = false;
-        uint32_t x = 0;
-        if (i < s) {
-          x = T.list[i];
-          uint32_t w = T.W[x];
-          rm = st_of(w) == ST_R && r12_violates(w, T.dist[x], rules, kl, h, cs, ubd);
+      for (uint32_t i0 = 0; i0 < s; i0 += BT * SCS_LIST_UNROLL) {
+        uint32_t x[SCS_LIST_UNROLL], w[SCS_LIST_UNROLL], d[SCS_LIST_UNROLL];
+#pragma unroll
+        for (int j = 0; j < SCS_LIST_UNROLL; j++) {
+          const uint32_t i = i0 + BT * j + t;
+          x[j] = i < s ? T.list[i] : SENT;
         }
-        warp_append(rm, x, &sh.cnt[1], T.tmp);
+#pragma unroll
+        for (int j = 0; j < SCS_LIST_UNROLL; j++) {
+          const uint32_t xx = x[j] != SENT ? x[j] : 0u;
+          w[j] = T.W[xx];
+          d[j] = T.dist[xx];
+        }
+#pragma unroll
+        for (int j = 0; j < SCS_LIST_UNROLL; j++) {
+          const bool rm = x[j] != SENT && st_of(w[j]) == ST_R &&
+                          r12_violates(w[j], d[j], rules, kl, h, cs, ubd);
+          warp_append(rm, x[j], &sh.cnt[1], T.tmp);
+        }
       }
       __syncthreads();
       const uint32_t nr = sh.cnt[1];
@@ -709,7 +791,16 @@ __device__ void rule12(Task &T, Sh &sh, bool test) {
         if (live(T.W[nb])) atomicSub(&T.W[nb], 1u);
       });
 #else
-      {
+      if (SCS_CHUNK_WORDS > 0) {
+        if (PROF_R12)
+          for (uint32_t i = t; i < nr; i += BT) {
+            const uint32_t x = T.tmp[i];
+            atomicAdd(&sh.cnt4[1], (unsigned long long)(T.off[x + 1] - T.off[x]));
+          }
+        warp_rows_chunked(T, T.tmp, nr, [&](uint32_t nb) { return live(T.W[nb]); },
+                          [&](uint32_t nb) { atomicSub(&T.W[nb], 1u); });
+        __syncthreads();
+      } else {
         // short rows one thread each (16-byte loads), long rows a warp each
         uint32_t *longs = T.tmp + sh.stride;
         for (uint32_t i0 = 0; i0 < nr; i0 += BT) {
@@ -955,17 +1046,22 @@ __device__ void choose_ustar(Task &T, Sh &sh) {
   unsigned long long c0 = SCS_PROF_MODE == 3 ? clock64() : 0;
   if (t == 0) sh.cnt[0] = 0;
   __syncthreads();
-  for (uint32_t i0 = 0; i0 < s; i0 += BT) {
-    uint32_t i = i0 + t;
-    bool c = false;
-    uint32_t x = 0;
-    if (i < s) {
-      x = T.list[i];
-      uint32_t w = T.W[x];
-      c = st_of(w) == ST_R && dc_of(w) > 0;
+  for (uint32_t i0 = 0; i0 < s; i0 += BT * SCS_LIST_UNROLL) {
+    uint32_t x[SCS_LIST_UNROLL], w[SCS_LIST_UNROLL];
+#pragma unroll
+    for (int j = 0; j < SCS_LIST_UNROLL; j++) {
+      const uint32_t i = i0 + BT * j + t;
+      x[j] = i < s ? T.list[i] : SENT;
     }
-    // candidates carry their list position: (i << 16) | x (both < 2^16)
-    warp_append(c, (i << 16) | x, &sh.cnt[0], T.tmp);
+#pragma unroll
+    for (int j = 0; j < SCS_LIST_UNROLL; j++) w[j] = T.W[x[j] != SENT ? x[j] : 0u];
+#pragma unroll
+    for (int j = 0; j < SCS_LIST_UNROLL; j++) {
+      const uint32_t i = i0 + BT * j + t;
+      const bool c = x[j] != SENT && st_of(w[j]) == ST_R && dc_of(w[j]) > 0;
+      // candidates carry their list position: (i << 16) | x (both < 2^16)
+      warp_append(c, (i << 16) | (x[j] & 0xFFFFu), &sh.cnt[0], T.tmp);
+    }
   }
   __syncthreads();
   const uint32_t nc = sh.cnt[0];

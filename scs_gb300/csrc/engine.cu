@@ -216,7 +216,10 @@ static int engine_init(scs_engine *E) {
   E->grid = (uint32_t)E->num_sms * cps;
   // per-CTA scratch
   Scratch &sc = E->scr;
-  sc.stride = n + 4;
+  // every per-task index is a local id or a list position, both below
+  // min(n, MAX_LOCAL): size the per-CTA arrays by that, not by n
+  const uint32_t n_loc = std::min<uint32_t>(n, MAX_LOCAL);
+  sc.stride = n_loc + 4;
   RC(E->dalloc(&sc.word, (size_t)E->grid * sc.stride));
   RC(E->dalloc(&sc.list, (size_t)E->grid * 2 * sc.stride, false));
   RC(E->dalloc(&sc.aux, (size_t)E->grid * sc.stride));
@@ -232,7 +235,7 @@ static int engine_init(scs_engine *E) {
   uint64_t avail_words = (uint64_t)(free_b * 0.85) / 4;
   if (!pw) pw = std::min<uint64_t>(avail_words / 4, 1ull << 33);
   if (!sw) {
-    uint64_t want = std::max<uint64_t>(1ull << 20, (uint64_t)(2 * n + 5) * 4096);
+    uint64_t want = std::max<uint64_t>(1ull << 20, (uint64_t)(2 * n_loc + 5) * 4096);
     uint64_t cap = (avail_words - std::min(pw, avail_words)) / E->grid;
     sw = std::min(want, cap);
   }
