@@ -108,6 +108,7 @@ struct Sh {
   unsigned long long rec;
   uint32_t red_u[NWARP];
   uint32_t red_u2[NWARP];
+  uint32_t red4[SCS_LIST_UNROLL * NWARP];  // per-row warp counts (compaction)
   double red_d[NWARP];
   uint32_t cl[CL_CAP];
   uint32_t A[CL_CAP];
@@ -495,16 +496,27 @@ __device__ void load_record(const uint32_t *rec, Task &T, Sh &sh) {
   const uint32_t *deg = rec + REC_HDR + s;
   if (t == 0) sh.cnt[0] = 0;
   __syncthreads();
-  for (uint32_t i = t; i < s; i += BT) {
+  for (uint32_t i0 = 0; i0 < s; i0 += BT * SCS_LIST_UNROLL) {
     // records may have been written by another SM: read through L2 so no
     // stale L1 line of an earlier neighbour in the arena is used
-    uint32_t e = __ldcg(ent + i), dg = __ldcg(deg + i);
-    uint32_t id = e >> 1, c = e & 1u;
-    T.W[id] = ((c ? ST_C : ST_R) << 30) | ((dg >> 16) << 15) | (dg & 0xFFFFu);
-    T.list[i] = id;
-    if (c) {
-      uint32_t k = atomicAdd(&sh.cnt[0], 1u);
-      if (k < CL_CAP) sh.cl[k] = id;
+    uint32_t e[SCS_LIST_UNROLL], dg[SCS_LIST_UNROLL];
+#pragma unroll
+    for (int j = 0; j < SCS_LIST_UNROLL; j++) {
+      const uint32_t i = i0 + BT * j + t;
+      e[j] = i < s ? __ldcg(ent + i) : SENT;
+      dg[j] = i < s ? __ldcg(deg + i) : 0u;
+    }
+#pragma unroll
+    for (int j = 0; j < SCS_LIST_UNROLL; j++) {
+      if (e[j] == SENT) continue;
+      const uint32_t i = i0 + BT * j + t;
+      const uint32_t id = e[j] >> 1, c = e[j] & 1u;
+      T.W[id] = ((c ? ST_C : ST_R) << 30) | ((dg[j] >> 16) << 15) | (dg[j] & 0xFFFFu);
+      T.list[i] = id;
+      if (c) {
+        uint32_t k = atomicAdd(&sh.cnt[0], 1u);
+        if (k < CL_CAP) sh.cl[k] = id;
+      }
     }
   }
   __syncthreads();
@@ -660,25 +672,37 @@ __device__ void compact_list(Task &T, Sh &sh, Keep keep) {
   const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
   const uint32_t s = sh.s;
   uint32_t out = 0;
-  for (uint32_t i0 = 0; i0 < s; i0 += BT) {
-    uint32_t i = i0 + t;
-    uint32_t x = 0;
-    bool k = false;
-    if (i < s) {
-      x = T.list[i];
-      k = keep(x);
+  // SCS_LIST_UNROLL rows of BT entries per round, one barrier per round:
+  // row j's survivors follow those of rows < j, so the order is kept
+  for (uint32_t i0 = 0; i0 < s; i0 += BT * SCS_LIST_UNROLL) {
+    uint32_t x[SCS_LIST_UNROLL];
+    bool k[SCS_LIST_UNROLL];
+    unsigned m[SCS_LIST_UNROLL];
+#pragma unroll
+    for (int j = 0; j < SCS_LIST_UNROLL; j++) {
+      const uint32_t i = i0 + BT * j + t;
+      x[j] = i < s ? T.list[i] : SENT;
     }
-    unsigned m = __ballot_sync(0xffffffffu, k);
-    if (lane == 0) sh.red_u[wid] = __popc(m);
+#pragma unroll
+    for (int j = 0; j < SCS_LIST_UNROLL; j++) {
+      k[j] = x[j] != SENT && keep(x[j]);
+      m[j] = __ballot_sync(0xffffffffu, k[j]);
+      if (lane == 0) sh.red4[j * NWARP + wid] = __popc(m[j]);
+    }
     __syncthreads();
-    uint32_t before = 0, tot = 0;
-    for (int q = 0; q < NWARP; q++) {
-      uint32_t c = sh.red_u[q];
-      if (q < wid) before += c;
-      tot += c;
+    uint32_t base = out;
+#pragma unroll
+    for (int j = 0; j < SCS_LIST_UNROLL; j++) {
+      uint32_t before = 0, tot = 0;
+      for (int q = 0; q < NWARP; q++) {
+        const uint32_t c = sh.red4[j * NWARP + q];
+        if (q < wid) before += c;
+        tot += c;
+      }
+      if (k[j]) T.list2[base + before + __popc(m[j] & ((1u << lane) - 1u))] = x[j];
+      base += tot;
     }
-    if (k) T.list2[out + before + __popc(m & ((1u << lane) - 1u))] = x;
-    out += tot;
+    out = base;
     __syncthreads();
   }
   uint32_t *tmpp = T.list;
@@ -867,9 +891,24 @@ __device__ void bounds(Task &T, Sh &sh) {
   if (sh.rules & R_PRUN2) {
     for (uint32_t i = t; i <= cs; i += BT) sh.hist[i] = 0;
     __syncthreads();
-    for (uint32_t i = t; i < sh.s; i += BT) {
-      uint32_t w = T.W[T.list[i]];
-      if (st_of(w) == ST_R) atomicAdd(&sh.hist[min(dc_of(w), cs)], 1u);
+    // Most R vertices fall into a few low bins: lanes with the same bin add
+    // once through their leader.
+    for (uint32_t i0 = 0; i0 < sh.s; i0 += BT * SCS_LIST_UNROLL) {
+      uint32_t x[SCS_LIST_UNROLL], w[SCS_LIST_UNROLL];
+#pragma unroll
+      for (int j = 0; j < SCS_LIST_UNROLL; j++) {
+        const uint32_t i = i0 + BT * j + t;
+        x[j] = i < sh.s ? T.list[i] : SENT;
+      }
+#pragma unroll
+      for (int j = 0; j < SCS_LIST_UNROLL; j++) w[j] = T.W[x[j] != SENT ? x[j] : 0u];
+#pragma unroll
+      for (int j = 0; j < SCS_LIST_UNROLL; j++) {
+        const bool r = x[j] != SENT && st_of(w[j]) == ST_R;
+        const uint32_t bin = r ? min(dc_of(w[j]), cs) : UINT32_MAX;
+        const unsigned grp = __match_any_sync(0xffffffffu, bin);
+        if (r && lane == __ffs(grp) - 1) atomicAdd(&sh.hist[bin], (uint32_t)__popc(grp));
+      }
     }
     // rank sort of C degrees into A (ascending)
     for (uint32_t i = t; i < cs; i += BT) {
@@ -1402,20 +1441,34 @@ __device__ void write_children(Task &T, Sh &sh, uint32_t code_lo,
                                uint32_t code_hi, uint32_t *const *dst) {
   const int t = threadIdx.x;
   const uint32_t s = sh.s, k = sh.ndoms;
-  for (uint32_t i = t; i < s; i += BT) {
-    const uint32_t x = T.list[i];
-    const uint32_t a = T.aux[x];
-    const uint32_t w = T.W[x];
-    for (uint32_t code = code_lo; code <= code_hi; code++) {
-      uint32_t *d = dst[code];
-      if (!d || child_skip(a, code, k)) continue;
-      uint32_t s2, c2;
-      child_shape(sh, code, s2, c2);
-      uint32_t o = i - skipped_before(sh, i, code);
-      uint32_t ent, deg;
-      child_entry(x, w, a, code, k, ent, deg);
-      d[REC_HDR + o] = ent;
-      d[REC_HDR + s2 + o] = deg;
+  for (uint32_t i0 = 0; i0 < s; i0 += BT * SCS_LIST_UNROLL) {
+    uint32_t xs[SCS_LIST_UNROLL], as[SCS_LIST_UNROLL], ws[SCS_LIST_UNROLL];
+#pragma unroll
+    for (int j = 0; j < SCS_LIST_UNROLL; j++) {
+      const uint32_t i = i0 + BT * j + t;
+      xs[j] = i < s ? T.list[i] : SENT;
+    }
+#pragma unroll
+    for (int j = 0; j < SCS_LIST_UNROLL; j++) {
+      const uint32_t xx = xs[j] != SENT ? xs[j] : 0u;
+      as[j] = T.aux[xx];
+      ws[j] = T.W[xx];
+    }
+#pragma unroll
+    for (int j = 0; j < SCS_LIST_UNROLL; j++) {
+      const uint32_t i = i0 + BT * j + t;
+      if (xs[j] == SENT) continue;
+      for (uint32_t code = code_lo; code <= code_hi; code++) {
+        uint32_t *d = dst[code];
+        if (!d || child_skip(as[j], code, k)) continue;
+        uint32_t s2, c2;
+        child_shape(sh, code, s2, c2);
+        uint32_t o = i - skipped_before(sh, i, code);
+        uint32_t ent, deg;
+        child_entry(xs[j], ws[j], as[j], code, k, ent, deg);
+        d[REC_HDR + o] = ent;
+        d[REC_HDR + s2 + o] = deg;
+      }
     }
   }
   if (t == 0) {
