@@ -146,9 +146,10 @@ int scs_stats(scs_engine *e, uint64_t *out);
 /* Search-kernel profile (16 u64): clock cycles spent per step phase summed
  * over CTAs [0 load, 1 min degree + rule 3, 2 rules 1/2, 3 bounds, 4 ustar,
  * 5 doms, 6 children, 7 other], then rule-1/2 rounds, rule-3 rounds, steps,
- * rule-1/2 cycles in [check passes, removal scans, compaction], removed
- * vertices and the row words their removal scanned.  The last five are zero
- * unless the library was built with -DSCS_PROF_MODE=1. */
+ * then five sub-phase counters: with -DSCS_PROF_MODE=1, rule-1/2 cycles in
+ * [check passes, removal rounds, recount rounds], removed vertices and
+ * recount rounds (modes 2-5 of bnb.cu measure other splits; the default
+ * build leaves them zero). */
 int scs_profile(scs_engine *e, uint64_t *out);
 
 /* Text of the last error on this engine (or the last creation failure). */

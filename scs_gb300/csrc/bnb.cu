@@ -66,8 +66,8 @@ constexpr int NWARP = BT / 32;
 // What the four sub-phase counters of scs_profile measure (they cost a few
 // per cent, so the default build leaves them at zero):
 // 0 nothing,
-// 1 rule-1/2 sub-phases (check passes, removal scans, compaction; removed
-//   vertices and their row words),
+// 1 rule-1/2 sub-phases (check passes, removal rounds, recount rounds;
+//   removed vertices and recount rounds),
 // 2 step cycles by task size at entry (s < 512, s < 4096, larger; step
 //   counts of the first two buckets),
 // 3 ustar sub-phases (candidate collection, score push, argmax; summed |C|
@@ -806,7 +806,10 @@ __device__ void rule12(Task &T, Sh &sh, bool test) {
           if (lane == 0) T.W[y] = (wy & ~DMASK) | c;
         }
         __syncthreads();
-        if (PROF_R12 && t == 0) sh.sub[1] += clock64() - c0;
+        if (PROF_R12 && t == 0) {
+          sh.sub[2] += clock64() - c0;
+          sh.cnt4[1]++;
+        }
         continue;
       }
       // neighbours lose one R neighbour each (non-returning reductions)
@@ -816,11 +819,6 @@ __device__ void rule12(Task &T, Sh &sh, bool test) {
       });
 #else
       if (SCS_CHUNK_WORDS > 0) {
-        if (PROF_R12)
-          for (uint32_t i = t; i < nr; i += BT) {
-            const uint32_t x = T.tmp[i];
-            atomicAdd(&sh.cnt4[1], (unsigned long long)(T.off[x + 1] - T.off[x]));
-          }
         warp_rows_chunked(T, T.tmp, nr, [&](uint32_t nb) { return live(T.W[nb]); },
                           [&](uint32_t nb) { atomicSub(&T.W[nb], 1u); });
         __syncthreads();
@@ -834,7 +832,6 @@ __device__ void rule12(Task &T, Sh &sh, bool test) {
           if (i < nr) {
             x = T.tmp[i];
             const uint32_t b = T.off[x], e = T.off[x + 1];
-            if (PROF_R12) atomicAdd(&sh.cnt4[1], (unsigned long long)(e - b));
             if (e - b > SCS_LANE_ROW)
               lng = true;
             else
@@ -867,7 +864,7 @@ __device__ void rule12(Task &T, Sh &sh, bool test) {
   }
   if (t == 0) {
     sh.nR = sh.s - sh.csize;
-    if (PROF_R12) sh.sub[2] += clock64() - c1;
+    if (PROF_R12) sh.sub[3] += clock64() - c1;
   }
   __syncthreads();
 }

@@ -278,8 +278,8 @@ class Engine:
         arr = (C.c_uint64 * 16)()
         self._check(lib().scs_profile(self._h, arr), "scs_profile")
         names = ["load", "mindeg_rule3", "rules12", "bounds", "ustar", "doms", "children",
-                 "other", "r12_rounds", "r3_rounds", "steps", "r12_check", "r12_remove",
-                 "r12_compact", "removed", "removed_row_words"]
+                 "other", "r12_rounds", "r3_rounds", "steps", "sub_cycles0", "sub_cycles1",
+                 "sub_cycles2", "sub_count0", "sub_count1"]
         return {nm: int(arr[i]) for i, nm in enumerate(names)}
 
     # ---- test hooks ----
