@@ -178,6 +178,25 @@ int scs_greedy_incumbent(uint32_t n, const uint32_t *off, const uint32_t *adj,
 /* Distance bound ubD from n(k, D) (main.cu:154-172). */
 uint32_t scs_distance_bound(uint32_t kl, uint32_t h);
 
+/* Check an answer community H[0..hs) of query (l, h, q) against a CSR graph
+ * (the checks the reference's results imply but never perform: it reports
+ * only the degree, main.cu:328-334).  Returns SCS_CHECK_OK when every id is
+ * below n, no id repeats, q is in H, l <= |H| <= h and H is connected;
+ * otherwise the first failed check.  *md receives the minimum degree inside
+ * H whenever the ids are valid (0 otherwise). */
+enum {
+  SCS_CHECK_OK = 0,
+  SCS_CHECK_EMPTY = 1,
+  SCS_CHECK_RANGE = 2,      /* an id >= n */
+  SCS_CHECK_REPEAT = 3,     /* an id listed twice */
+  SCS_CHECK_NO_QUERY = 4,   /* q not in H */
+  SCS_CHECK_SIZE = 5,       /* |H| outside [l, h] */
+  SCS_CHECK_DISCONNECTED = 6
+};
+int scs_check_community(uint32_t n, const uint32_t *off, const uint32_t *adj,
+                        const uint32_t *H, uint32_t hs, uint32_t q, uint32_t l,
+                        uint32_t h, uint32_t *md);
+
 /* ---- server surface (host only) ---- */
 
 /* Parse one queue message (main.cu:92-109): returns 0 and fills q for

@@ -15,7 +15,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU = ["prep.cu", "bnb.cu", "engine.cu", "noalloc.cu"]
 CXX = ["host_graph.cpp", "host_api.cpp"]
 LIB = "libscs.so"
-EXES = {"scs_server": "server.cpp", "scs_client": "client.cpp"}
+EXES = {"scs_server": "server.cpp", "scs_client": "client.cpp", "scs_verify": "verify.cpp"}
 
 
 def nvcc():
@@ -74,7 +74,8 @@ def _build(verbose, force, defines):
         list(ex.map(run, cmds))
     objs = [os.path.join(objdir, f + ".o") for f in CU + CXX]
     run([nvcc(), *ARCH, "-shared", "-o", out, *objs, "-lcudart", "-lpthread"])
-    # reference-compatible server and batch client, linked to the library
+    # reference-compatible server and batch client, and the answer verifier,
+    # linked to the library
     for exe, src in EXES.items():
         run(["g++", "-O2", "-std=c++17", "-Wall", "-o", os.path.join(OUT, exe),
              os.path.join(CSRC, src), "-L" + OUT, "-lscs", "-Wl,-rpath,$ORIGIN",

@@ -1,7 +1,9 @@
 // host_api.cpp -- host-only entry points of include/scs.h (no GPU needed).
+#include <algorithm>
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "../../include/scs.h"
 #include "host_graph.h"
@@ -27,6 +29,50 @@ int scs_read_edge_list(const char *path, uint32_t *n, uint64_t *nnz,
 }
 
 void scs_free(void *p) { free(p); }
+
+int scs_check_community(uint32_t n, const uint32_t *off, const uint32_t *adj,
+                        const uint32_t *H, uint32_t hs, uint32_t q, uint32_t l,
+                        uint32_t h, uint32_t *md) {
+  if (md) *md = 0;
+  if (!off || !adj || (hs && !H)) return SCS_EINVAL;
+  if (hs == 0) return SCS_CHECK_EMPTY;
+  std::vector<uint32_t> mem(H, H + hs);
+  for (uint32_t v : mem)
+    if (v >= n) return SCS_CHECK_RANGE;
+  std::sort(mem.begin(), mem.end());
+  if (std::adjacent_find(mem.begin(), mem.end()) != mem.end()) return SCS_CHECK_REPEAT;
+  auto index = [&](uint32_t v) -> int64_t {
+    auto it = std::lower_bound(mem.begin(), mem.end(), v);
+    return (it != mem.end() && *it == v) ? (int64_t)(it - mem.begin()) : -1;
+  };
+  // minimum degree inside H, and connectivity by a DFS over H
+  uint32_t mind = UINT32_MAX;
+  for (uint32_t v : mem) {
+    uint32_t d = 0;
+    for (uint32_t k = off[v]; k < off[v + 1]; k++) d += index(adj[k]) >= 0;
+    mind = std::min(mind, d);
+  }
+  if (md) *md = mind;
+  if (index(q) < 0) return SCS_CHECK_NO_QUERY;
+  if (mem.size() < l || mem.size() > h) return SCS_CHECK_SIZE;
+  std::vector<char> vis(mem.size(), 0);
+  std::vector<uint32_t> stack{mem[0]};
+  vis[0] = 1;
+  size_t cnt = 1;
+  while (!stack.empty()) {
+    const uint32_t v = stack.back();
+    stack.pop_back();
+    for (uint32_t k = off[v]; k < off[v + 1]; k++) {
+      const int64_t i = index(adj[k]);
+      if (i >= 0 && !vis[i]) {
+        vis[i] = 1;
+        cnt++;
+        stack.push_back(adj[k]);
+      }
+    }
+  }
+  return cnt == mem.size() ? SCS_CHECK_OK : SCS_CHECK_DISCONNECTED;
+}
 
 int scs_core_decompose(uint32_t n, const uint32_t *off, const uint32_t *adj,
                        uint32_t *core) {

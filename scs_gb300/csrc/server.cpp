@@ -15,6 +15,11 @@
 // memory.  The listener blocks in msgrcv instead of polling.
 //
 // SCS_IPC_PROJ (environment) overrides the ftok project character (tests).
+// SCS_COMMUNITIES (environment, any non-empty value) also writes each answer
+// community to results/communities_<graph file name>, one row per query:
+// "QID|N1|N2|Degree|Status|v1 v2 ..." (global vertex ids, status as in
+// include/scs.h); scs_verify checks that file against the graph.  The
+// reference computes these communities but never outputs them.
 #include <sys/ipc.h>
 #include <sys/msg.h>
 #include <sys/stat.h>
@@ -113,6 +118,11 @@ int main(int argc, const char *argv[]) {
   std::string fname = "results/results_" + (pos == std::string::npos ? gp : gp.substr(pos + 1));
   mkdir("results", 0775);
   if (!file_exists(fname)) append_line(fname, "N1|N2|QID|Time|Degree|Overtime|Heu|TotalTime");
+  const char *want_h = getenv("SCS_COMMUNITIES");
+  const bool write_h = want_h && *want_h;
+  const std::string hname =
+      "results/communities_" + (pos == std::string::npos ? gp : gp.substr(pos + 1));
+  if (write_h && !file_exists(hname)) append_line(hname, "QID|N1|N2|Degree|Status|Community");
 
   scs_config cfg{};
   cfg.limit_queries = (uint32_t)limit_queries;
@@ -152,6 +162,8 @@ int main(int argc, const char *argv[]) {
   uint64_t outstanding = 0;
   uint64_t next_query_id = 0;
   std::vector<scs_result> res(256);
+  const uint32_t h_stride = 512;  // queries need h < 510
+  std::vector<uint32_t> hbuf(write_h ? res.size() * h_stride : 0);
   bool quit = false;
   for (;;) {
     // take messages
@@ -191,13 +203,24 @@ int main(int argc, const char *argv[]) {
       }
     }
     int k;
-    while ((k = scs_poll(E, res.data(), (int)res.size(), nullptr, 0)) > 0) {
+    while ((k = scs_poll(E, res.data(), (int)res.size(), write_h ? hbuf.data() : nullptr,
+                         h_stride)) > 0) {
       for (int i = 0; i < k; i++) {
         const scs_result &r = res[i];
         if (r.status == SCS_BAD_QUERY) {
           std::cout << "Client wrong input parameters! Query ID: " << r.ticket << std::endl;
         } else {
           append_line(fname, scs_format_row(r));
+          if (write_h) {
+            std::string row = std::to_string(r.q) + "|" + std::to_string(r.l) + "|" +
+                              std::to_string(r.h) + "|" + std::to_string(r.degree) + "|" +
+                              std::to_string(r.status) + "|";
+            for (uint32_t j = 0; j < std::min(r.h_size, h_stride); j++) {
+              if (j) row += ' ';
+              row += std::to_string(hbuf[(size_t)i * h_stride + j]);
+            }
+            append_line(hname, row);
+          }
           std::cout << "Found Solution : " << "QID = " << r.q << ", N1 = " << r.l
                     << ", N2 = " << r.h << ", kl = " << r.degree << std::endl;
         }

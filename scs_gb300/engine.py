@@ -90,6 +90,8 @@ def lib(build_if_missing=False):
                                        C.c_uint32, _u32p, _u32p, _u32p]
     L.scs_distance_bound.argtypes = [C.c_uint32, C.c_uint32]
     L.scs_distance_bound.restype = C.c_uint32
+    L.scs_check_community.argtypes = [C.c_uint32, _u32p, _u32p, _u32p, C.c_uint32, C.c_uint32,
+                                      C.c_uint32, C.c_uint32, _u32p]
     L.scs_local_graph_noalloc.argtypes = [vp, vp, vp, C.c_uint32, C.c_uint32, C.c_uint32,
                                           C.c_uint32, C.c_uint32, vp, vp, vp, vp,
                                           C.c_uint64, vp, vp]
@@ -160,6 +162,24 @@ def greedy_incumbent(n, off, adj, l, h, q):
 
 def distance_bound(kl, h):
     return int(lib().scs_distance_bound(kl, h))
+
+
+CHECK_REASONS = {0: "ok", 1: "empty", 2: "id out of range", 3: "repeated id",
+                 4: "query vertex missing", 5: "size outside [l, h]", 6: "not connected"}
+
+
+def check_community(n, off, adj, H, q, l, h):
+    """(code, min degree) of community H for query (l, h, q); code 0 = valid
+    (ids in range and distinct, q in H, l <= |H| <= h, connected)."""
+    off = np.ascontiguousarray(off, dtype=np.uint32)
+    adj = np.ascontiguousarray(adj, dtype=np.uint32)
+    H = np.ascontiguousarray(H, dtype=np.uint32)
+    md = C.c_uint32()
+    rc = lib().scs_check_community(n, _p(off), _p(adj), _p(H) if len(H) else None, len(H),
+                                   q, l, h, C.byref(md))
+    if rc < 0:
+        raise SCSError("scs_check_community failed (%d)" % rc)
+    return rc, md.value
 
 
 NOALLOC_MAX_N = 1 << 19

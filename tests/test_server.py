@@ -109,7 +109,8 @@ def test_client_sends_reference_messages(tmp_path):
 @pytest.mark.gpu
 def test_server_end_to_end(tmp_path, chunglu_small):
     """scs_server with the reference CLI answers queries sent by scs_client
-    and writes the reference's results file; degrees equal the oracle's."""
+    and writes the reference's results file; degrees equal the oracle's, and
+    the communities it writes on request pass scs_verify."""
     from scs_gb300 import build as B
     B.build()
     gold = [g for g in json.load(open(os.path.join(GOLD, "answers_chunglu_n4000.json")))["queries"]
@@ -117,7 +118,7 @@ def test_server_end_to_end(tmp_path, chunglu_small):
     qf = tmp_path / "queries.txt"
     qf.write_text("".join("%d %d %d %d %d\n" % (g["l"], g["h"], g["q"], g["heur"], g["limit_doms"])
                           for g in gold) + "1 2\nserver_exit\n")
-    env = dict(os.environ, SCS_IPC_PROJ="s")
+    env = dict(os.environ, SCS_IPC_PROJ="s", SCS_COMMUNITIES="1")
     srv = subprocess.Popen([B.exe_path("scs_server"), chunglu_small, "300000", "100000", "0.5",
                             "1", "8", "100", "1", "1", "1", "1", "1"],
                            cwd=str(tmp_path), env=env, stdout=subprocess.PIPE,
@@ -142,3 +143,8 @@ def test_server_end_to_end(tmp_path, chunglu_small):
         g = want[(int(f[0]), int(f[1]), int(f[2]))]
         assert int(f[4]) == g["degree"]
         assert f[5] == "0" and f[6] == ("1" if g["heu_hit"] else "0")
+    comm = tmp_path / "results" / "communities_chunglu_n4000.txt"
+    v = subprocess.run([B.exe_path("scs_verify"), chunglu_small, str(comm)],
+                       capture_output=True, text=True, timeout=120)
+    assert v.returncode == 0, v.stdout + v.stderr
+    assert "verified %d of %d rows" % (len(gold), len(gold)) in v.stdout
