@@ -169,6 +169,13 @@ void scs_free(void *p);
 int scs_core_decompose(uint32_t n, const uint32_t *off, const uint32_t *adj,
                        uint32_t *core);
 
+/* The same core numbers computed on GPU `device` by level-synchronous
+ * peeling (replaces the serial start-up peeling, src/Graph.h:82-109; the
+ * engine uses it at creation).  Allocates its own device buffers.  Returns
+ * 0, SCS_EINVAL for an invalid CSR or SCS_ECUDA. */
+int scs_core_decompose_gpu(uint32_t n, const uint32_t *off, const uint32_t *adj,
+                           uint32_t *core, int device);
+
 /* Greedy incumbent kl = max(heu2, heu3, heu4) and its community
  * (CSSC_heu, inc/heuristic.h:321-349).  H needs room for max(h, deg(q)+1). */
 int scs_greedy_incumbent(uint32_t n, const uint32_t *off, const uint32_t *adj,

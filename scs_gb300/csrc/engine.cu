@@ -155,7 +155,27 @@ static int engine_init(scs_engine *E) {
   RC(E->dalloc(&E->d_core, n, false));
   CK(cudaMemcpyAsync(E->d_off, g.off.data(), (n + 1) * 4ull, cudaMemcpyHostToDevice, E->stream));
   if (nnz) CK(cudaMemcpyAsync(E->d_adj, g.adj.data(), nnz * 4ull, cudaMemcpyHostToDevice, E->stream));
-  CK(cudaMemcpyAsync(E->d_core, g.core.data(), n * 4ull, cudaMemcpyHostToDevice, E->stream));
+  {
+    // core numbers by GPU peeling (core.cu), copied back for admission and
+    // the host-side incumbent; the scratch is released right away
+    uint32_t *scr = nullptr;
+    void *ctr = nullptr, *hctr = nullptr;
+    cudaError_t e0 = cudaMalloc((void **)&scr, std::max<size_t>(3ull * n, 1) * 4);
+    if (e0 == cudaSuccess) e0 = cudaMalloc(&ctr, 16);
+    if (e0 == cudaSuccess) e0 = cudaMallocHost(&hctr, 16);
+    int ce = e0 == cudaSuccess ? gpu_core_numbers(E->d_off, E->d_adj, n, E->d_core, scr, ctr,
+                                                   hctr, E->num_sms, E->stream)
+                               : (int)e0;
+    E->g.core.resize(n);
+    if (ce == 0 && n)
+      ce = (int)cudaMemcpyAsync(E->g.core.data(), E->d_core, n * 4ull, cudaMemcpyDeviceToHost,
+                                E->stream);
+    if (ce == 0) ce = (int)cudaStreamSynchronize(E->stream);
+    cudaFree(scr);
+    cudaFree(ctr);
+    if (hctr) cudaFreeHost(hctr);
+    if (ce) return E->cuda_fail((cudaError_t)ce, "core numbers");
+  }
   // slots
   E->nslots = c.limit_queries ? c.limit_queries : 64;
   E->slots.resize(E->nslots);
@@ -530,7 +550,7 @@ static int create_common(scs_engine **out, scs_engine *E, const scs_config *cfg)
 int scs_create(scs_engine **out, const char *path, const scs_config *cfg) {
   if (!out || !path) return SCS_EINVAL;
   scs_engine *E = new scs_engine();
-  int rc = load_edge_list(path, E->g, E->err);
+  int rc = load_edge_list(path, E->g, E->err, /*with_core=*/false);
   if (rc) {
     g_create_error = E->err;
     delete E;
@@ -544,7 +564,7 @@ int scs_create_csr(scs_engine **out, uint32_t n, const uint32_t *off,
                    const uint32_t *adj, const scs_config *cfg) {
   if (!out) return SCS_EINVAL;
   scs_engine *E = new scs_engine();
-  if (adopt_csr(n, off, adj, E->g, E->err)) {
+  if (adopt_csr(n, off, adj, E->g, E->err, /*with_core=*/false)) {
     g_create_error = E->err;
     delete E;
     *out = nullptr;

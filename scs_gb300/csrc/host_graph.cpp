@@ -114,7 +114,7 @@ int build_csr(uint32_t n, std::vector<std::vector<uint64_t>> &parts,
 
 }  // namespace
 
-int load_edge_list(const char *path, HostGraph &g, std::string &err) {
+int load_edge_list(const char *path, HostGraph &g, std::string &err, bool with_core) {
   FILE *f = fopen(path, "rb");
   if (!f) {
     err = std::string("cannot open ") + path;
@@ -167,12 +167,12 @@ int load_edge_list(const char *path, HostGraph &g, std::string &err) {
   int rc = build_csr((uint32_t)n64, parts, g, err);
   if (rc) return rc;
   g.m_header = m64;
-  finish_graph(g);
+  finish_graph(g, with_core);
   return 0;
 }
 
 int adopt_csr(uint32_t n, const uint32_t *off, const uint32_t *adj,
-              HostGraph &g, std::string &err) {
+              HostGraph &g, std::string &err, bool with_core) {
   if (!off || (n && !adj)) {
     err = "null CSR";
     return -1;
@@ -201,11 +201,11 @@ int adopt_csr(uint32_t n, const uint32_t *off, const uint32_t *adj,
   g.off.assign(off, off + n + 1);
   g.adj.assign(adj, adj + off[n]);
   g.m_header = off[n] / 2;
-  finish_graph(g);
+  finish_graph(g, with_core);
   return 0;
 }
 
-void finish_graph(HostGraph &g) {
+void finish_graph(HostGraph &g, bool with_core) {
   const uint32_t n = g.n;
   g.degree.resize(n);
   g.dmax = 0;
@@ -215,6 +215,10 @@ void finish_graph(HostGraph &g) {
   }
   // bin-sort peeling (core numbers are unique; src/Graph.h:82-109 computes
   // the same array with a bucket list)
+  if (!with_core) {
+    g.core.clear();
+    return;
+  }
   g.core.assign(n, 0);
   if (!n) return;
   std::vector<uint32_t> deg(g.degree), bin(g.dmax + 2, 0), vert(n), pos(n);

@@ -18,12 +18,13 @@ struct HostGraph {
 
 // Edge-list load with the reference's semantics (src/Graph.h:5-67).
 // Returns 0, or a negative code with a message in err.
-int load_edge_list(const char *path, HostGraph &g, std::string &err);
+// with_core = false leaves g.core empty (the engine computes it on the GPU).
+int load_edge_list(const char *path, HostGraph &g, std::string &err, bool with_core = true);
 // Validate a caller CSR and adopt it.
 int adopt_csr(uint32_t n, const uint32_t *off, const uint32_t *adj,
-              HostGraph &g, std::string &err);
-// Degrees, dmax and core numbers (bin-sort peeling).
-void finish_graph(HostGraph &g);
+              HostGraph &g, std::string &err, bool with_core = true);
+// Degrees, dmax and (with_core) core numbers by bin-sort peeling.
+void finish_graph(HostGraph &g, bool with_core = true);
 
 // Per-thread work arrays for the greedy incumbent; reused across queries.
 struct HeuWork {

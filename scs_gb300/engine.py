@@ -86,6 +86,7 @@ def lib(build_if_missing=False):
     L.scs_read_edge_list.argtypes = [C.c_char_p, _u32p, _u64p, C.POINTER(_u32p), C.POINTER(_u32p)]
     L.scs_free.argtypes = [vp]
     L.scs_core_decompose.argtypes = [C.c_uint32, _u32p, _u32p, _u32p]
+    L.scs_core_decompose_gpu.argtypes = [C.c_uint32, _u32p, _u32p, _u32p, C.c_int]
     L.scs_greedy_incumbent.argtypes = [C.c_uint32, _u32p, _u32p, C.c_uint32, C.c_uint32,
                                        C.c_uint32, _u32p, _u32p, _u32p]
     L.scs_distance_bound.argtypes = [C.c_uint32, C.c_uint32]
@@ -145,6 +146,18 @@ def core_numbers(n, off, adj):
     if rc:
         raise SCSError("scs_core_decompose failed (%d)" % rc)
     return core
+
+
+def core_numbers_gpu(n, off, adj, device=0):
+    """Core numbers by GPU peeling (scs_core_decompose_gpu); equal to
+    core_numbers()."""
+    off = np.ascontiguousarray(off, dtype=np.uint32)
+    adj = np.ascontiguousarray(adj, dtype=np.uint32)
+    core = np.zeros(max(n, 1), dtype=np.uint32)
+    rc = lib().scs_core_decompose_gpu(n, _p(off), _p(adj) if len(adj) else None, _p(core), device)
+    if rc:
+        raise SCSError("scs_core_decompose_gpu failed (%d)" % rc)
+    return core[:n]
 
 
 def greedy_incumbent(n, off, adj, l, h, q):
