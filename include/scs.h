@@ -36,6 +36,7 @@ extern "C" {
 #define SCS_ENOMEM -4     /* device or host allocation failed */
 #define SCS_EBUSY -5      /* no free query slot */
 #define SCS_ENOTREADY -6  /* nothing finished yet */
+#define SCS_ESTALL -7     /* a host worker made no progress (scs_last_error) */
 
 /* ---- per-query result status (scs_result.status) ---- */
 #define SCS_DONE 0          /* search finished: degree is the optimum */
@@ -139,7 +140,10 @@ enum {
   SCS_STAT_PREP_NS = 8,   /* device time inside preprocessing */
   SCS_STAT_LAUNCHES = 9,  /* kernel launches issued */
   SCS_STAT_H2D = 10,      /* host-to-device bytes copied by the engine */
-  SCS_STAT_D2H = 11       /* device-to-host bytes copied by the engine */
+  SCS_STAT_D2H = 11,      /* device-to-host bytes copied by the engine */
+  SCS_STAT_HEUR_NS = 12   /* time admission waited for a greedy incumbent with
+                             the GPU idle (incumbents are computed by background
+                             host threads; ready queries are admitted first) */
 };
 int scs_stats(scs_engine *e, uint64_t *out);
 

@@ -587,13 +587,6 @@ __device__ void eval_mindeg(Task &T, Sh &sh, bool test, uint32_t *t_wit) {
   __syncthreads();
 }
 
-__device__ __forceinline__ void refresh_kl(Task &T, Sh &sh, bool test) {
-  if (!test && threadIdx.x == 0) {
-    uint32_t g = *(volatile uint32_t *)&T.slot->kl;
-    if (g > sh.kl) sh.kl = g;
-  }
-  __syncthreads();
-}
 
 // ---------------------------------------------------------------------------
 // rule 3 to a fixpoint: every R neighbour of a C vertex with dC+dR == kl+1
@@ -724,7 +717,6 @@ __device__ void rule12(Task &T, Sh &sh, bool test) {
   uint32_t removed = 0;
   if (rules & (R_RED1 | R_RED2)) {
     for (;;) {
-      refresh_kl(T, sh, test);
       const uint32_t kl = sh.kl, cs = sh.csize, s = sh.s;
       const uint32_t ubd = ubd_dev(kl, h);
       unsigned long long c0 = clock64();
@@ -1535,7 +1527,6 @@ __device__ void step_core(Task &T, Sh &sh, bool test, uint32_t *t_wit) {
   }
   __syncthreads();
   phase_mark(sh, 7);
-  refresh_kl(T, sh, test);
   if (sh.csize > sh.h) {
     if (t == 0) sh.outcome = 1;
     __syncthreads();
@@ -1543,7 +1534,6 @@ __device__ void step_core(Task &T, Sh &sh, bool test, uint32_t *t_wit) {
   }
   if (sh.l <= sh.csize) eval_mindeg(T, sh, test, t_wit);
   if (sh.rules & R_RED3) {
-    refresh_kl(T, sh, test);
     const uint32_t c0 = sh.csize;
     rule3(T, sh);
     if (sh.csize > sh.h) {
@@ -1563,7 +1553,6 @@ __device__ void step_core(Task &T, Sh &sh, bool test, uint32_t *t_wit) {
   phase_mark(sh, 2);
   bounds(T, sh);
   phase_mark(sh, 3);
-  refresh_kl(T, sh, test);
   uint32_t ub = min(sh.p1, sh.p2);
   if (ub <= sh.kl) {
     if (t == 0) sh.outcome = 2;
@@ -1636,6 +1625,7 @@ __device__ void set_task_header(const SearchParams &P, Sh &sh,
     sh.ldoms = min(sl->limit_doms, (uint32_t)MAX_DOMS);
     sh.rules = sl->rules;
     sh.kl = *(volatile uint32_t *)&sl->kl;
+    sh.wit_pending = *(volatile uint32_t *)&sl->abort;
     sh.q_local = sl->q_local;
     sh.dmax = P.g.dmax;
     sh.mean_deg = sl->n_local ? (float)P.sa.loc_off[(size_t)sh.slot * (P.sa.stride_n + 1) + sl->n_local] /
@@ -1924,9 +1914,7 @@ search_kernel(SearchParams P) {
       }
       __syncthreads();
       if (sh.stop) break;
-      set_task_header(P, sh, rec);
-      if (t == 0) sh.wit_pending = *(volatile uint32_t *)&P.slots[sh.slot].abort;
-      __syncthreads();
+      set_task_header(P, sh, rec);  // also reads the query's abort flag
       if (sh.wit_pending) {
         if (t == 0) finish_tasks(P, sh.slot, -1);
         __syncthreads();
@@ -1940,7 +1928,14 @@ search_kernel(SearchParams P) {
       phase_mark(sh, 0);
     }
     // ---------------- one step ----------------
-    if (t == 0) sh.wit_pending = *(volatile uint32_t *)&P.slots[sh.slot].abort;
+    // The query's abort flag and incumbent, read together once per step: a
+    // stale incumbent only prunes less, so the step does not re-read it.
+    if (t == 0) {
+      const volatile Slot *sl = P.slots + sh.slot;
+      const uint32_t ab = sl->abort, g = sl->kl;
+      sh.wit_pending = ab;
+      if (g > sh.kl) sh.kl = g;
+    }
     __syncthreads();
     if (sh.wit_pending) {  // the query stopped (budget / capacity): drop
       if (t == 0) {

@@ -14,6 +14,8 @@
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <condition_variable>
+#include <memory>
 #include <cstdio>
 #include <cstring>
 #include <deque>
@@ -40,6 +42,16 @@ struct Pending {
   scs_query q;
   uint64_t ticket;
   uint64_t t_submit;
+};
+
+// A submitted query and its greedy incumbent, computed in the background by
+// the heuristic workers so that it overlaps the search of earlier queries.
+struct Job {
+  Pending p;
+  bool bad = false;   // rejected at submission
+  bool done = false;  // kl/H ready (guarded by scs_engine::heu_mu)
+  uint32_t kl = 0, ku = 0;
+  std::vector<uint32_t> H;
 };
 
 struct SlotHost {
@@ -90,7 +102,12 @@ struct scs_engine {
   Counters *d_ctr = nullptr;
   uint32_t rules = 31;
   // host state
-  std::deque<Pending> queue;
+  std::deque<std::shared_ptr<Job>> queue;     // admission order
+  std::deque<std::shared_ptr<Job>> heu_todo;  // incumbents not yet started
+  std::mutex heu_mu;
+  std::condition_variable heu_cv, heu_done_cv;
+  std::vector<std::thread> heu_workers;
+  bool heu_stop = false;
   std::deque<Done> done;
   uint64_t next_ticket = 1;
   uint32_t running = 0;
@@ -131,6 +148,30 @@ struct scs_engine {
     int r_ = (call);        \
     if (r_) return r_;      \
   } while (0)
+
+// Background worker: greedy incumbents of submitted queries, in submission
+// order (the graph is read-only after creation; work[tid] is this worker's).
+static void heu_worker(scs_engine *E, unsigned tid) {
+  for (;;) {
+    std::shared_ptr<Job> j;
+    {
+      std::unique_lock<std::mutex> lk(E->heu_mu);
+      E->heu_cv.wait(lk, [&] { return E->heu_stop || !E->heu_todo.empty(); });
+      if (E->heu_stop) return;
+      j = E->heu_todo.front();
+      E->heu_todo.pop_front();
+    }
+    std::vector<uint32_t> H;
+    const uint32_t kl = greedy_incumbent(E->g, j->p.q.l, j->p.q.h, j->p.q.q, E->work[tid], H);
+    {
+      std::lock_guard<std::mutex> lk(E->heu_mu);
+      j->kl = kl;
+      j->H.swap(H);
+      j->done = true;
+    }
+    E->heu_done_cv.notify_all();
+  }
+}
 
 static int engine_init(scs_engine *E) {
   const scs_config &c = E->cfg;
@@ -275,6 +316,8 @@ static int engine_init(scs_engine *E) {
   E->host_threads = c.host_threads ? c.host_threads
                                    : std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
   E->work.resize(E->host_threads);
+  // greedy incumbents of submitted queries are computed by these workers
+  for (unsigned k = 0; k < E->host_threads; k++) E->heu_workers.emplace_back(heu_worker, E, k);
   return 0;
 }
 
@@ -345,48 +388,41 @@ static int admit(scs_engine *E) {
   std::vector<uint32_t> free_slots;
   for (uint32_t i = 0; i < E->nslots; i++)
     if (!E->slots[i].busy) free_slots.push_back(i);
-  std::vector<Pending> batch;
-  while (!E->queue.empty() && batch.size() < free_slots.size() &&
-         batch.size() < E->prep_cap) {
-    batch.push_back(E->queue.front());
-    E->queue.pop_front();
+  // Admit the queued queries whose incumbents are ready, in queue order;
+  // the others keep computing in the background while the admitted ones
+  // search.  Only with nothing on the GPU does admission wait (for one).
+  std::vector<std::shared_ptr<Job>> batch;
+  {
+    std::unique_lock<std::mutex> lk(E->heu_mu);
+    if (E->running == 0 && !E->queue.empty()) {
+      const uint64_t t0 = now_ns();
+      auto any_done = [&] {
+        for (auto &j : E->queue)
+          if (j->done) return true;
+        return false;
+      };
+      if (!E->heu_done_cv.wait_for(lk, std::chrono::minutes(10), any_done)) {
+        E->err = "greedy incumbent workers made no progress for 10 minutes";
+        return SCS_ESTALL;
+      }
+      E->stats[SCS_STAT_HEUR_NS] += now_ns() - t0;
+    }
+    for (auto it = E->queue.begin();
+         it != E->queue.end() && batch.size() < free_slots.size() && batch.size() < E->prep_cap;) {
+      if ((*it)->done) {
+        batch.push_back(*it);
+        it = E->queue.erase(it);
+      } else {
+        ++it;
+      }
+    }
   }
   if (batch.empty()) return 0;
-  const uint32_t n = E->g.n;
-  struct Adm {
-    bool bad = false;
-    uint32_t kl = 0, ku = 0;
-    std::vector<uint32_t> H;
-  };
-  std::vector<Adm> adm(batch.size());
-  // greedy incumbents on host threads
-  {
-    std::atomic<size_t> next{0};
-    auto worker = [&](unsigned tid) {
-      for (;;) {
-        size_t i = next.fetch_add(1);
-        if (i >= batch.size()) break;
-        const scs_query &q = batch[i].q;
-        Adm &a = adm[i];
-        if (q.q >= n || q.h < 1 || q.h >= CL_CAP - 1 || q.l > q.h) {
-          a.bad = true;
-          continue;
-        }
-        a.ku = std::min(E->g.core[q.q], q.h - 1);
-        if (q.heuristic) a.kl = greedy_incumbent(E->g, q.l, q.h, q.q, E->work[tid], a.H);
-      }
-    };
-    unsigned nt = std::min<unsigned>(E->host_threads, (unsigned)batch.size());
-    std::vector<std::thread> th;
-    for (unsigned k = 1; k < nt; k++) th.emplace_back(worker, k);
-    worker(0);
-    for (auto &t : th) t.join();
-  }
   std::vector<PrepJob> jobs;
   size_t fs = 0;
   for (size_t i = 0; i < batch.size(); i++) {
-    const Pending &p = batch[i];
-    Adm &a = adm[i];
+    const Pending &p = batch[i]->p;
+    Job &a = *batch[i];
     if (a.bad) {
       finish_now(E, p, 0, SCS_BAD_QUERY, 0, {});
       continue;
@@ -423,7 +459,7 @@ static int admit(scs_engine *E) {
   E->stats[SCS_STAT_H2D] += jobs.size() * sizeof(PrepJob);
   cudaEventRecord(E->ev2, E->stream);
   prep_kernel<<<(unsigned)jobs.size(), PREP_THREADS, 0, E->stream>>>(
-      DevGraph{n, E->g.dmax, E->d_off, E->d_adj, E->d_core}, E->sa, E->d_slots,
+      DevGraph{E->g.n, E->g.dmax, E->d_off, E->d_adj, E->d_core}, E->sa, E->d_slots,
       E->d_jobs, (int)jobs.size(), E->ps, E->pool, E->d_ctr);
   cudaEventRecord(E->ev3, E->stream);
   E->prep_pending = true;
@@ -589,12 +625,27 @@ int scs_core_numbers(scs_engine *E, uint32_t *core) {
 
 int scs_submit(scs_engine *E, const scs_query *q, uint64_t *ticket) {
   if (!E || !q) return SCS_EINVAL;
-  Pending p;
-  p.q = *q;
-  p.ticket = E->next_ticket++;
-  p.t_submit = now_ns();
-  E->queue.push_back(p);
-  if (ticket) *ticket = p.ticket;
+  auto j = std::make_shared<Job>();
+  j->p.q = *q;
+  j->p.ticket = E->next_ticket++;
+  j->p.t_submit = now_ns();
+  if (q->q >= E->g.n || q->h < 1 || q->h >= CL_CAP - 1 || q->l > q->h) {
+    j->bad = true;
+    j->done = true;
+  } else {
+    j->ku = std::min(E->g.core[q->q], q->h - 1);
+    if (!q->heuristic) {
+      j->done = true;  // kl = 0
+    } else {
+      {
+        std::lock_guard<std::mutex> lk(E->heu_mu);
+        E->heu_todo.push_back(j);
+      }
+      E->heu_cv.notify_one();
+    }
+  }
+  E->queue.push_back(j);
+  if (ticket) *ticket = j->p.ticket;
   return 0;
 }
 
@@ -650,6 +701,12 @@ const char *scs_last_error(scs_engine *E) {
 
 int scs_destroy(scs_engine *E) {
   if (!E) return SCS_EINVAL;
+  {
+    std::lock_guard<std::mutex> lk(E->heu_mu);
+    E->heu_stop = true;
+  }
+  E->heu_cv.notify_all();
+  for (auto &t : E->heu_workers) t.join();
   if (E->stream) cudaStreamSynchronize(E->stream);
   for (void *p : E->allocs) cudaFree(p);
   if (E->ev0) cudaEventDestroy(E->ev0);

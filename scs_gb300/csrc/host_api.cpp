@@ -90,7 +90,7 @@ int scs_greedy_incumbent(uint32_t n, const uint32_t *off, const uint32_t *adj,
   if (!kl || q >= n) return SCS_EINVAL;
   HostGraph g;
   std::string err;
-  if (adopt_csr(n, off, adj, g, err)) return SCS_EINVAL;
+  if (adopt_csr(n, off, adj, g, err, /*with_core=*/false)) return SCS_EINVAL;
   HeuWork w;
   std::vector<uint32_t> out;
   *kl = greedy_incumbent(g, l, h, q, w, out);
