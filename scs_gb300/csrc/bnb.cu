@@ -1812,6 +1812,9 @@ __device__ void stack_make_room(const SearchParams &P, uint32_t *sbase,
     unsigned long long cnt = min(shift, used - base);
     for (unsigned long long i = threadIdx.x; i < cnt; i += BT)
       sbase[base + i] = __ldcg(sbase + b0 + base + i);
+    // the next chunk and later reads use L2 loads: each thread's moved words
+    // must have reached L2 (a barrier alone only orders them within the CTA)
+    __threadfence();
     __syncthreads();
   }
   __syncthreads();
@@ -2002,10 +2005,27 @@ search_kernel(SearchParams P) {
             P.slots[sh.slot].status = RS_CAPACITY;
           }
         }
+        // Count the reserved children before any of them is published: a
+        // child spilled to the pool can be taken and finished by another CTA
+        // before this step ends, and the query must not reach zero
+        // outstanding tasks (and be reported done) while its siblings are
+        // still stored.
+        uint32_t nres = 0;
+        for (uint32_t code = 1; code <= k + 1; code++) nres += sh.kid_dst[code] != 0;
+        if (nres) finish_tasks(P, sh.slot, (long long)nres);
       }
       __syncthreads();
       if (k + 1 >= 1) {
         write_children(T, sh, 1, k + 1, (uint32_t *const *)sh.kid_dst);
+        // Every thread stored entries of the children.  Records are read
+        // back with L2 loads -- by another SM after thread 0 publishes a
+        // spilled child, by this CTA when it pops one from its stack -- so
+        // each thread fences its own stores before the barrier (a fence
+        // orders only the calling thread's writes; a barrier only makes them
+        // visible within the CTA).
+        bool wrote = false;
+        for (uint32_t code = 1; code <= k + 1; code++) wrote |= sh.kid_dst[code] != 0;
+        if (wrote) __threadfence();
         __syncthreads();
         for (uint32_t code = 1; code <= k + 1; code++) {
           if (!sh.kid_dst[code]) continue;
@@ -2015,7 +2035,6 @@ search_kernel(SearchParams P) {
             if (sh.kid_len[code] & 0x80000000u) publish_pool(P, sh.kid_pool[code]);
             sh.bytes += 16ull * s2;
           }
-          pushed++;
         }
       }
       uint32_t s2, c2;
@@ -2031,6 +2050,8 @@ search_kernel(SearchParams P) {
     }
     phase_mark(sh, 6);
     if (t == 0) {
+      // the parent ends; the in-place Include child (pushed == 1) replaces
+      // it (the other children were counted when reserved)
       finish_tasks(P, sh.slot, (long long)pushed - 1);
       Slot *sl = P.slots + sh.slot;
       unsigned long long nd = atomicAdd(&sl->nodes, 1ull) + 1ull;
@@ -2061,6 +2082,7 @@ search_kernel(SearchParams P) {
       const uint32_t *src = sbase + s_bot;
       const uint32_t len = __ldcg(src + 3);
       for (uint32_t i = t; i < len; i += BT) s_rec[i] = __ldcg(src + i);
+      __threadfence();  // every copying thread, before thread 0 publishes
       __syncthreads();
       if (t == 0) {
         if (publish_pool(P, s_pool_off)) {
@@ -2107,6 +2129,7 @@ search_kernel(SearchParams P) {
             d[3] = len;
             d[REC_HDR + 2 * sh.s] = len;
           }
+          __threadfence();  // every writer: the record is read back with L2 loads
           __syncthreads();
           if (t == 0 && s_pool_rec) publish_pool(P, s_pool_off);
         } else if (t == 0) {

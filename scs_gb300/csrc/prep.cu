@@ -126,8 +126,11 @@ prep_kernel(DevGraph g, SlotArrays sa, Slot *slots, const PrepJob *jobs,
       sl->pending = 0;
     }
   }
-  __syncthreads();
+  // every thread fences its own stores of the root record and slot fields
+  // before the barrier; thread 0 then publishes (a fence orders only the
+  // calling thread's writes)
   __threadfence();
+  __syncthreads();
   if (t == 0) {
     sl->state = SLOT_SEARCH;
     if (job.root_to_pool) {
