@@ -91,6 +91,7 @@ struct Sh {
   uint32_t ustar, us_idx;
   uint32_t ndoms, ndom_cand;
   uint32_t masked;  // this step's scores came from C-neighbour masks
+  uint32_t bad_rec;  // load_record met an entry id outside the local graph
   uint32_t doms[MAX_DOMS];
   uint32_t doms_idx[MAX_DOMS];
   uint32_t wit_pending;
@@ -494,7 +495,10 @@ __device__ void load_record(const uint32_t *rec, Task &T, Sh &sh) {
   const uint32_t s = sh.s;
   const uint32_t *ent = rec + REC_HDR;
   const uint32_t *deg = rec + REC_HDR + s;
-  if (t == 0) sh.cnt[0] = 0;
+  if (t == 0) {
+    sh.cnt[0] = 0;
+    sh.bad_rec = 0;
+  }
   __syncthreads();
   for (uint32_t i0 = 0; i0 < s; i0 += BT * SCS_LIST_UNROLL) {
     // records may have been written by another SM: read through L2 so no
@@ -511,6 +515,10 @@ __device__ void load_record(const uint32_t *rec, Task &T, Sh &sh) {
       if (e[j] == SENT) continue;
       const uint32_t i = i0 + BT * j + t;
       const uint32_t id = e[j] >> 1, c = e[j] & 1u;
+      if (id >= sh.n_local) {  // never index state with it; the caller stops
+        sh.bad_rec = 1;
+        continue;
+      }
       T.W[id] = ((c ? ST_C : ST_R) << 30) | ((dg[j] >> 16) << 15) | (dg[j] & 0xFFFFu);
       T.list[i] = id;
       if (c) {
@@ -1757,10 +1765,14 @@ __device__ bool publish_pool(const SearchParams &P, unsigned long long off) {
 }
 
 // Header sanity of a task record (thread 0): slot in range and searching,
-// 1 <= s <= n_local, csize <= s, len == 2s+5, footer == len, first and last
-// entry ids in range.  Returns 0 or a code naming the first failed check.
+// 1 <= s <= n_local, csize <= s, len == 2s+5, the record inside the region
+// it came from (room words: the length its stack footer gave, or what is
+// left of the pool arena), footer == len, first and last entry ids in range.
+// Returns 0 or a code naming the first failed check.  No word outside the
+// region is read.
 __device__ uint32_t check_record(const SearchParams &P, const uint32_t *rec,
-                                 int from_pool) {
+                                 int from_pool, unsigned long long room) {
+  if (room < REC_HDR + 1) return 10;
   uint32_t slot = __ldcg(rec), s = __ldcg(rec + 1), cs = __ldcg(rec + 2),
            len = __ldcg(rec + 3);
   if (slot >= P.nslots) return 1;
@@ -1770,12 +1782,12 @@ __device__ uint32_t check_record(const SearchParams &P, const uint32_t *rec,
   if (s == 0 || s > nl) return 3;
   if (cs > s) return 4;
   if (len != 2 * s + 5) return 5;
+  if (len > room || (!from_pool && len != room)) return 9;
   if (__ldcg(rec + REC_HDR + 2 * s) != len) return 6;
   // first and last entry ids in range (the full ascending check is O(s) on
   // one thread and is not paid per task)
   if ((__ldcg(rec + REC_HDR) >> 1) >= nl) return 7;
   if ((__ldcg(rec + REC_HDR + s - 1) >> 1) >= nl) return 8;
-  (void)from_pool;
   return 0;
 }
 
@@ -1834,6 +1846,7 @@ search_kernel(SearchParams P) {
   __shared__ uint32_t *s_rec;
   __shared__ unsigned long long s_pool_off;
   __shared__ int s_pool_rec;
+  __shared__ unsigned long long s_room;  // words of the popped stack record
   __shared__ unsigned long long s_deadline;
   const uint32_t cta = blockIdx.x;
   const int t = threadIdx.x;
@@ -1871,6 +1884,7 @@ search_kernel(SearchParams P) {
             s_top = s_bot;
           } else {
             s_rec = sbase + (s_top - len);
+            s_room = len;
             s_top -= len;
           }
         }
@@ -1905,7 +1919,9 @@ search_kernel(SearchParams P) {
       const uint32_t *rec = s_rec;
       if (t == 0) {
         // validate the record before trusting any index in it
-        uint32_t bad = check_record(P, rec, s_pool_rec);
+        const unsigned long long room =
+            s_pool_rec ? P.pool.arena_cap - (unsigned long long)(rec - P.pool.arena) : s_room;
+        uint32_t bad = check_record(P, rec, s_pool_rec, room);
         if (bad) {
           atomicOr(&P.ctr->error, ERR_RECORD);
           P.ctr->err_info[0] = bad;
@@ -1926,6 +1942,16 @@ search_kernel(SearchParams P) {
       phase_mark(sh, 7);
       T = make_task(P, sh, dyn, cta);
       load_record(rec, T, sh);
+      if (sh.bad_rec) {  // a damaged record: report it and leave the slice
+        if (t == 0) {
+          atomicOr(&P.ctr->error, ERR_RECORD);
+          P.ctr->err_info[0] = 11;
+          P.ctr->err_info[1] = sh.slot;
+          P.ctr->err_info[2] = sh.s;
+          P.ctr->err_info[3] = sh.n_local;
+        }
+        break;
+      }
       if (t == 0) sh.have = 1;
       __syncthreads();
       phase_mark(sh, 0);
