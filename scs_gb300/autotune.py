@@ -46,9 +46,9 @@ def autotune(n, off, adj, rows, node_budget, grid=DEFAULT_GRID, use_cache=True,
             pass
     trials = []
     for cps, slice_us in grid:
+        # task store sized from device memory, as for the measured engine
         eng = Engine(csr=(n, off, adj), limit_queries=len(rows), ctas_per_sm=cps,
-                     slice_us=slice_us, node_budget=node_budget, stack_words=1 << 22,
-                     pool_words=1 << 28, device=device)
+                     slice_us=slice_us, node_budget=node_budget, device=device)
         t0 = time.perf_counter()
         res = eng.solve(rows)
         dt = time.perf_counter() - t0
