@@ -492,8 +492,10 @@ static int slice(scs_engine *E) {
   Counters hc;
   CK(cudaMemcpyAsync(&hc, E->d_ctr, sizeof(Counters), cudaMemcpyDeviceToHost, E->stream));
   uint32_t ph[2];
+  unsigned long long arena_used = 0;
   CK(cudaMemcpyAsync(ph, E->pool.head, 4, cudaMemcpyDeviceToHost, E->stream));
   CK(cudaMemcpyAsync(ph + 1, E->pool.tail, 4, cudaMemcpyDeviceToHost, E->stream));
+  CK(cudaMemcpyAsync(&arena_used, E->pool.arena_top, 8, cudaMemcpyDeviceToHost, E->stream));
   CK(cudaStreamSynchronize(E->stream));
   float ms = 0;
   cudaEventElapsedTime(&ms, E->ev0, E->ev1);
@@ -553,8 +555,10 @@ static int slice(scs_engine *E) {
     E->stats[SCS_STAT_H2D] += sizeof(Slot);
     E->running--;
   }
-  // pool reset when fully drained
-  if (ph[0] >= std::min(ph[1], E->pool.desc_cap) && ph[1] > 0) {
+  // pool reset when fully drained: every published record taken, and
+  // something allocated (failed reservations also advance arena_top, so a
+  // full arena with nothing published is reset too)
+  if (ph[0] >= std::min(ph[1], E->pool.desc_cap) && (ph[1] > 0 || arena_used > 0)) {
     uint32_t used = std::min(ph[1], E->pool.desc_cap);
     CK(cudaMemsetAsync(E->pool.desc, 0, used * 8ull, E->stream));
     CK(cudaMemsetAsync(E->pool.arena_top, 0, 8, E->stream));
