@@ -318,7 +318,9 @@ def main():
                    "verified_fraction": verified / max(len(results), 1),
                    "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
                    "nodes": st1["nodes"] - st0["nodes"], "parallelism": "replicas" if world > 1 else "1 GPU",
-                   "ctas_per_sm": tune["ctas_per_sm"], "slice_us": tune["slice_us"]},
+                   "ctas_per_sm": tune["ctas_per_sm"],
+                   "resident_ctas": st1["ctas"], "smem_state_words": st1["smem_words"],
+                   "slice_us": tune["slice_us"]},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak if peak else None, "traffic": traffic,
                      "peak_kind": peak_kind, "kernel": "search_kernel",

@@ -141,9 +141,14 @@ enum {
   SCS_STAT_LAUNCHES = 9,  /* kernel launches issued */
   SCS_STAT_H2D = 10,      /* host-to-device bytes copied by the engine */
   SCS_STAT_D2H = 11,      /* device-to-host bytes copied by the engine */
-  SCS_STAT_HEUR_NS = 12   /* time admission waited for a greedy incumbent with
+  SCS_STAT_HEUR_NS = 12,  /* time admission waited for a greedy incumbent with
                              the GPU idle (incumbents are computed by background
                              host threads; ready queries are admitted first) */
+  SCS_STAT_CTAS = 13,     /* search CTAs resident per slice (SMs x CTAs per
+                             SM after the occupancy check) */
+  SCS_STAT_SMEM_WORDS = 14/* task state words held in shared memory per CTA
+                             (larger local graphs keep them in device memory) */
+  /* 15: device error flags seen so far (ERR_* bits, OR-ed) */
 };
 int scs_stats(scs_engine *e, uint64_t *out);
 

@@ -541,11 +541,13 @@ __device__ void clear_state(Task &T, Sh &sh) {
 __device__ void eval_mindeg(Task &T, Sh &sh, bool test, uint32_t *t_wit) {
   const int t = threadIdx.x;
   const uint32_t cs = sh.csize;
+  // read before block_min's barriers: thread 0 overwrites sh.best below
+  const uint32_t best0 = sh.best;
   uint32_t v = UINT32_MAX;
   for (uint32_t i = t; i < cs && i < CL_CAP; i += BT) v = min(v, dc_of(T.W[sh.cl[i]]));
   uint32_t md = block_min(v, sh);
   if (md == UINT32_MAX) return;
-  bool improve_step = (sh.best == UINT32_MAX || md > sh.best);
+  bool improve_step = (best0 == UINT32_MAX || md > best0);
   if (improve_step && t == 0) sh.best = md;
   if (test) {
     if (md > sh.kl && t == 0) sh.kl = md;
@@ -1720,7 +1722,7 @@ step_test_kernel(SearchParams P) {
 // search: persistent within a time slice
 // ---------------------------------------------------------------------------
 __device__ void finish_tasks(const SearchParams &P, uint32_t slot, long long delta) {
-  // delta = children pushed - 1 (per finished task); runs on thread 0
+  // delta = tasks created - tasks ended; runs on thread 0
   Slot *sl = P.slots + slot;
   unsigned long long old = atomicAdd(&sl->pending, (unsigned long long)delta);
   atomicAdd(&P.ctr->pending, (unsigned long long)delta);
@@ -1818,6 +1820,11 @@ __device__ void stack_make_room(const SearchParams &P, uint32_t *sbase,
                                 uint32_t len, unsigned long long &top,
                                 unsigned long long &bot) {
   unsigned long long t0 = top, b0 = bot;
+  // Thread 0 reserves records (moving top and bot) as soon as this returns:
+  // every thread must have read them first, or a late warp could see the new
+  // top, decide on a slide alone and run the copy loop's barriers out of
+  // step with the rest of the CTA.
+  __syncthreads();
   if (t0 + len <= P.stk.words || b0 == 0) return;
   const unsigned long long used = t0 - b0, shift = b0;
   for (unsigned long long base = 0; base < used; base += shift) {
@@ -1848,6 +1855,7 @@ search_kernel(SearchParams P) {
   __shared__ int s_pool_rec;
   __shared__ unsigned long long s_room;  // words of the popped stack record
   __shared__ unsigned long long s_deadline;
+  __shared__ int s_bad;  // the record just obtained failed its header checks
   const uint32_t cta = blockIdx.x;
   const int t = threadIdx.x;
   uint32_t *sbase = P.stk.base + (size_t)cta * P.stk.words;
@@ -1874,6 +1882,13 @@ search_kernel(SearchParams P) {
   for (;;) {
     // ---------------- obtain a task ----------------
     if (!sh.have) {
+      // Thread 0 rewrites s_rec and sh.stop below.  The idle path loops back
+      // here right after every thread read them, and the slice-exit check
+      // reads sh.stop just before: without this barrier a late warp could
+      // read the next iteration's record pointer (or stop flag), take the
+      // other branch and run one barrier out of step with the rest of the
+      // CTA from then on.
+      __syncthreads();
       if (t == 0) {
         s_rec = nullptr;
         s_pool_rec = 0;
@@ -1918,21 +1933,24 @@ search_kernel(SearchParams P) {
       if (!s_rec) continue;
       const uint32_t *rec = s_rec;
       if (t == 0) {
-        // validate the record before trusting any index in it
+        // validate the record before trusting any index in it (a flag of its
+        // own: other warps may still be reading sh.stop above)
         const unsigned long long room =
             s_pool_rec ? P.pool.arena_cap - (unsigned long long)(rec - P.pool.arena) : s_room;
         uint32_t bad = check_record(P, rec, s_pool_rec, room);
+        s_bad = bad != 0;
         if (bad) {
           atomicOr(&P.ctr->error, ERR_RECORD);
           P.ctr->err_info[0] = bad;
-          P.ctr->err_info[1] = rec[0];
-          P.ctr->err_info[2] = rec[1];
-          P.ctr->err_info[3] = rec[3];
-          sh.stop = 1;
+          if (room >= REC_HDR) {
+            P.ctr->err_info[1] = __ldcg(rec);
+            P.ctr->err_info[2] = __ldcg(rec + 1);
+            P.ctr->err_info[3] = __ldcg(rec + 3);
+          }
         }
       }
       __syncthreads();
-      if (sh.stop) break;
+      if (s_bad) break;
       set_task_header(P, sh, rec);  // also reads the query's abort flag
       if (sh.wit_pending) {
         if (t == 0) finish_tasks(P, sh.slot, -1);
@@ -1990,7 +2008,6 @@ search_kernel(SearchParams P) {
     }
 #endif
     local_nodes++;
-    uint32_t pushed = 0;
     bool cont = false;
     if (sh.outcome == 0) {
       const uint32_t k = sh.ndoms;
@@ -2035,23 +2052,27 @@ search_kernel(SearchParams P) {
         // child spilled to the pool can be taken and finished by another CTA
         // before this step ends, and the query must not reach zero
         // outstanding tasks (and be reported done) while its siblings are
-        // still stored.
+        // still stored.  The same update ends the parent and counts the
+        // in-place Include dive, so it can reach zero only when nothing of
+        // this task remains.
         uint32_t nres = 0;
         for (uint32_t code = 1; code <= k + 1; code++) nres += sh.kid_dst[code] != 0;
-        if (nres) finish_tasks(P, sh.slot, (long long)nres);
+        uint32_t s0, c0;
+        child_shape(sh, 0, s0, c0);
+        const long long delta = (long long)nres + (child_alive(sh, s0, c0) ? 1 : 0) - 1;
+        if (delta) finish_tasks(P, sh.slot, delta);
       }
       __syncthreads();
       if (k + 1 >= 1) {
         write_children(T, sh, 1, k + 1, (uint32_t *const *)sh.kid_dst);
-        // Every thread stored entries of the children.  Records are read
-        // back with L2 loads -- by another SM after thread 0 publishes a
-        // spilled child, by this CTA when it pops one from its stack -- so
-        // each thread fences its own stores before the barrier (a fence
-        // orders only the calling thread's writes; a barrier only makes them
-        // visible within the CTA).
-        bool wrote = false;
-        for (uint32_t code = 1; code <= k + 1; code++) wrote |= sh.kid_dst[code] != 0;
-        if (wrote) __threadfence();
+        // Every thread stored entries of the children.  A child spilled to
+        // the pool is read by another SM once thread 0 publishes it, so each
+        // thread fences its own stores before the barrier.  Children on the
+        // stack are read back only by this CTA, after the barrier.
+        bool spilled = false;
+        for (uint32_t code = 1; code <= k + 1; code++)
+          spilled |= sh.kid_dst[code] != 0 && (sh.kid_len[code] & 0x80000000u);
+        if (spilled) __threadfence();
         __syncthreads();
         for (uint32_t code = 1; code <= k + 1; code++) {
           if (!sh.kid_dst[code]) continue;
@@ -2069,16 +2090,15 @@ search_kernel(SearchParams P) {
       if (cont) {
         if (t == 0) sh.bytes += 16ull * s2;
         apply_include(T, sh);
-        pushed++;
       } else {
         clear_aux_list(T, sh);
       }
     }
     phase_mark(sh, 6);
     if (t == 0) {
-      // the parent ends; the in-place Include child (pushed == 1) replaces
-      // it (the other children were counted when reserved)
-      finish_tasks(P, sh.slot, (long long)pushed - 1);
+      // a task that did not branch ends here (a branching one was settled
+      // with its children)
+      if (sh.outcome != 0) finish_tasks(P, sh.slot, -1);
       Slot *sl = P.slots + sh.slot;
       unsigned long long nd = atomicAdd(&sl->nodes, 1ull) + 1ull;
       if (sl->node_budget && nd >= sl->node_budget && !sl->abort) {
@@ -2186,7 +2206,5 @@ search_kernel(SearchParams P) {
     }
   }
 }
-
-size_t search_static_smem() { return sizeof(Sh) + 64; }
 
 }  // namespace scs

@@ -256,14 +256,26 @@ static int engine_init(scs_engine *E) {
   CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_regs, search_kernel, SEARCH_THREADS, 0));
   uint32_t cps = c.ctas_per_sm ? c.ctas_per_sm : (uint32_t)SEARCH_MINB;
   if (occ_regs >= 1) cps = std::min<uint32_t>(cps, (uint32_t)occ_regs);
-  size_t stat = search_static_smem();
-  size_t per_sm = 228 * 1024;
-  size_t budget = std::min((size_t)max_optin, per_sm / cps - 1024);
+  // The dynamic region gets what is left of the SM's shared memory per CTA
+  // after the kernel's own static shared memory (as built, not estimated: a
+  // few bytes too many silently cost a whole CTA per SM) and the per-block
+  // reservation.
+  cudaFuncAttributes fattr{};
+  CK(cudaFuncGetAttributes(&fattr, search_kernel));
+  int per_sm_i = 0, reserved_i = 0;
+  CK(cudaDeviceGetAttribute(&per_sm_i, cudaDevAttrMaxSharedMemoryPerMultiprocessor, E->dev));
+  CK(cudaDeviceGetAttribute(&reserved_i, cudaDevAttrReservedSharedMemoryPerBlock, E->dev));
+  const size_t stat = fattr.sharedSizeBytes;
+  const size_t per_cta = (size_t)per_sm_i / cps;
+  size_t budget = std::min((size_t)max_optin + (size_t)reserved_i, per_cta);
+  budget = budget > (size_t)reserved_i ? budget - (size_t)reserved_i : 0;
   size_t words = budget > stat ? (budget - stat) / 4 : 0;
   E->nw_smem = (uint32_t)std::min<size_t>(words, std::min<uint32_t>(n, MAX_LOCAL));
   E->smem_bytes = (size_t)E->nw_smem * 4;
   CK(cudaFuncSetAttribute(search_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                           (int)E->smem_bytes));
+  CK(cudaFuncSetAttribute(search_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                          (int)cudaSharedmemCarveoutMaxShared));
   CK(cudaFuncSetAttribute(step_test_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                           (int)E->smem_bytes));
   int occ = 0;
@@ -275,6 +287,8 @@ static int engine_init(scs_engine *E) {
   }
   cps = std::min<uint32_t>(cps, (uint32_t)occ);
   E->grid = (uint32_t)E->num_sms * cps;
+  E->stats[SCS_STAT_CTAS] = E->grid;
+  E->stats[SCS_STAT_SMEM_WORDS] = E->nw_smem;
   // per-CTA scratch
   Scratch &sc = E->scr;
   // every per-task index is a local id or a list position, both below

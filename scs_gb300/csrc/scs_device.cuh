@@ -213,6 +213,5 @@ int gpu_core_numbers(const uint32_t *d_off, const uint32_t *d_adj, uint32_t n,
                      uint32_t *d_core, uint32_t *d_scratch, void *ctr_dev,
                      void *ctr_host, int num_sms, cudaStream_t st);
 __global__ void step_test_kernel(SearchParams P);
-size_t search_static_smem();
 
 }  // namespace scs

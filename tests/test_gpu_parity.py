@@ -199,3 +199,18 @@ def test_results_same_alone_and_in_mix(eng_c1):
         alone = eng_c1.solve([row])[0]
         assert alone["degree"] == m["degree"]
         assert alone["status"] == m["status"]
+
+
+def test_default_occupancy_three_ctas_per_sm(rmat15):
+    """The search kernel's shared memory is sized from its static shared
+    memory as built, so the default three CTAs per SM are all resident (a
+    budget a few bytes too large silently dropped the engine to two)."""
+    import torch
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    e = _engine(graph=rmat15, limit_queries=4)
+    try:
+        st = e.stats()
+        assert st["ctas"] == 3 * sms, st
+        assert st["smem_words"] > 16000, st
+    finally:
+        e.close()
