@@ -1722,10 +1722,15 @@ step_test_kernel(SearchParams P) {
 // search: persistent within a time slice
 // ---------------------------------------------------------------------------
 __device__ void finish_tasks(const SearchParams &P, uint32_t slot, long long delta) {
-  // delta = tasks created - tasks ended; runs on thread 0
+  // delta = tasks created - tasks ended; runs on thread 0.  Only a decrease
+  // can finish the query, so only then is the old count waited for.
   Slot *sl = P.slots + slot;
-  unsigned long long old = atomicAdd(&sl->pending, (unsigned long long)delta);
   atomicAdd(&P.ctr->pending, (unsigned long long)delta);
+  if (delta >= 0) {
+    atomicAdd(&sl->pending, (unsigned long long)delta);
+    return;
+  }
+  unsigned long long old = atomicAdd(&sl->pending, (unsigned long long)delta);
   if ((long long)old + delta == 0) {
     sl->t_done = gtimer();
     __threadfence();
@@ -1856,6 +1861,14 @@ search_kernel(SearchParams P) {
   __shared__ unsigned long long s_room;  // words of the popped stack record
   __shared__ unsigned long long s_deadline;
   __shared__ int s_bad;  // the record just obtained failed its header checks
+  // Thread 0's view of the query and the slice, read together at each step's
+  // start (one round trip instead of one per check): the node count and
+  // budget decide the search budget, the idle-CTA count the donation, the
+  // stop flag the slice exit.  Each is at most one step stale, which only
+  // delays a budget stop or a donation by a step.  Shared, not registers:
+  // only thread 0 uses them, and registers are the kernel's tight resource.
+  __shared__ unsigned long long s_nodes_seen, s_budget_seen;
+  __shared__ uint32_t s_abort_seen, s_hungry_seen, s_stop_seen;
   const uint32_t cta = blockIdx.x;
   const int t = threadIdx.x;
   uint32_t *sbase = P.stk.base + (size_t)cta * P.stk.words;
@@ -1867,6 +1880,8 @@ search_kernel(SearchParams P) {
     s_top = P.stk.top[cta];
     s_bot = P.stk.bot[cta];
     s_hungry = 0;
+    s_nodes_seen = s_budget_seen = 0;
+    s_abort_seen = s_hungry_seen = s_stop_seen = 0;
     sh.have = 0;
     sh.stop = 0;
     sh.bytes = 0;
@@ -1980,6 +1995,11 @@ search_kernel(SearchParams P) {
     if (t == 0) {
       const volatile Slot *sl = P.slots + sh.slot;
       const uint32_t ab = sl->abort, g = sl->kl;
+      s_nodes_seen = sl->nodes;
+      s_budget_seen = sl->node_budget;
+      s_hungry_seen = *(volatile uint32_t *)&P.ctr->hungry;
+      s_stop_seen = *(volatile uint32_t *)&P.ctr->stop;
+      s_abort_seen = ab;
       sh.wit_pending = ab;
       if (g > sh.kl) sh.kl = g;
     }
@@ -2100,10 +2120,11 @@ search_kernel(SearchParams P) {
       // with its children)
       if (sh.outcome != 0) finish_tasks(P, sh.slot, -1);
       Slot *sl = P.slots + sh.slot;
-      unsigned long long nd = atomicAdd(&sl->nodes, 1ull) + 1ull;
-      if (sl->node_budget && nd >= sl->node_budget && !sl->abort) {
+      atomicAdd(&sl->nodes, 1ull);  // no return value: a reduction, no wait
+      if (s_budget_seen && s_nodes_seen + 1ull >= s_budget_seen && !s_abort_seen) {
         sl->status = RS_TIMEOUT;
         sl->abort = 1;
+        s_abort_seen = 1;
       }
       sh.have = cont ? 1 : 0;
     }
@@ -2112,7 +2133,7 @@ search_kernel(SearchParams P) {
     // ---------------- donate the oldest stack record if others are idle ----
     if (t == 0) {
       s_rec = nullptr;
-      if (*(volatile uint32_t *)&P.ctr->hungry > 0 && s_top > s_bot) {
+      if (s_hungry_seen > 0 && s_top > s_bot) {
         uint32_t len = __ldcg(sbase + s_bot + 3);
         if (len >= 5 && s_bot + len < s_top) {  // keep at least one record
           unsigned long long off = atomicAdd(P.pool.arena_top, (unsigned long long)len);
@@ -2140,7 +2161,7 @@ search_kernel(SearchParams P) {
     }
     // ---------------- leave the slice? ----------------
     if (t == 0) {
-      if (gtimer() > s_deadline || *(volatile uint32_t *)&P.ctr->stop) sh.stop = 1;
+      if (gtimer() > s_deadline || s_stop_seen) sh.stop = 1;
     }
     __syncthreads();
     if (sh.stop) {
