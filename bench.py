@@ -320,6 +320,7 @@ def main():
                    "nodes": st1["nodes"] - st0["nodes"], "parallelism": "replicas" if world > 1 else "1 GPU",
                    "ctas_per_sm": tune["ctas_per_sm"],
                    "resident_ctas": st1["ctas"], "smem_state_words": st1["smem_words"],
+                   "active_queries": st1["active"],
                    "slice_us": tune["slice_us"]},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak if peak else None, "traffic": traffic,

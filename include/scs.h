@@ -65,6 +65,9 @@ typedef struct {
                                  (stands in for the level cap main.cu:444) */
   uint32_t host_threads;      /* threads for the greedy incumbent (0: auto) */
   int32_t device;             /* CUDA device ordinal                      */
+  uint32_t active_queries;    /* queries searched at once; the other admitted
+                                 ones wait prepared (0: auto, 32). Fewer keep
+                                 the searched local graphs in L2. */
 } scs_config;
 
 /* One query: the reference's message fields (main.cu:92-119). */
@@ -127,7 +130,7 @@ int scs_poll(scs_engine *e, scs_result *out, int max, uint32_t *h_buf,
              uint32_t h_stride);
 
 /* Engine counters (array of SCS_STAT_COUNT u64). */
-#define SCS_STAT_COUNT 16
+#define SCS_STAT_COUNT 20
 enum {
   SCS_STAT_NODES = 0,     /* tasks processed */
   SCS_STAT_SLICES = 1,    /* search slices launched */
@@ -146,9 +149,11 @@ enum {
                              host threads; ready queries are admitted first) */
   SCS_STAT_CTAS = 13,     /* search CTAs resident per slice (SMs x CTAs per
                              SM after the occupancy check) */
-  SCS_STAT_SMEM_WORDS = 14/* task state words held in shared memory per CTA
+  SCS_STAT_SMEM_WORDS = 14,/* task state words held in shared memory per CTA
                              (larger local graphs keep them in device memory) */
-  /* 15: device error flags seen so far (ERR_* bits, OR-ed) */
+  SCS_STAT_ERRORS = 15,   /* device error flags seen so far (bits, OR-ed) */
+  SCS_STAT_ACTIVE = 16,   /* queries searched at once (the active target) */
+  SCS_STAT_RELEASES = 17  /* prepared queries released to the search */
 };
 int scs_stats(scs_engine *e, uint64_t *out);
 

@@ -56,6 +56,7 @@ struct Job {
 
 struct SlotHost {
   bool busy = false;
+  bool parked = false;  // prepared, root not yet released to the search
   Pending p;
   uint32_t kl_heu = 0;
   std::vector<uint32_t> heuH;
@@ -67,6 +68,9 @@ struct Done {
 };
 
 std::string g_create_error;
+
+// Queries searched at once unless scs_config.active_queries says otherwise.
+constexpr uint32_t SCS_DEFAULT_ACTIVE = 32;
 
 }  // namespace
 
@@ -98,6 +102,14 @@ struct scs_engine {
   size_t smem_bytes = 0;
   Pool pool{};
   Stacks stk{};
+  // Roots are parked at a fixed place per slot at the head of the pool arena
+  // (root_stride words each, root_words in all) and released a few at a time
+  // so that only active_target queries are searched at once.
+  unsigned long long root_stride = 0, root_words = 0;
+  std::deque<uint32_t> parked;  // release order (entries of collected slots are skipped)
+  uint32_t n_parked = 0;
+  uint32_t *d_rel = nullptr;
+  uint32_t active_target = 0;
   Scratch scr{};
   Counters *d_ctr = nullptr;
   uint32_t rules = 31;
@@ -318,9 +330,19 @@ static int engine_init(scs_engine *E) {
   RC(E->dalloc(&E->stk.base, (size_t)E->grid * sw, false));
   RC(E->dalloc(&E->stk.top, E->grid));
   RC(E->dalloc(&E->stk.bot, E->grid));
-  E->pool.arena_cap = pw;
-  RC(E->dalloc(&E->pool.arena, pw, false));
+  E->root_stride = 2ull * n_loc + 5;
+  E->root_words = (unsigned long long)E->nslots * E->root_stride;
+  E->pool.arena_cap = pw + E->root_words;
+  RC(E->dalloc(&E->pool.arena, E->pool.arena_cap, false));
   RC(E->dalloc(&E->pool.arena_top, 1));
+  // the bump area starts after the parked roots
+  CK(cudaMemcpyAsync(E->pool.arena_top, &E->root_words, 8, cudaMemcpyHostToDevice, E->stream));
+  RC(E->dalloc(&E->d_rel, E->nslots, false));
+  // Queries searched at once.  Fewer keep the active local graphs in L2 (the
+  // search is bound by dependent loads); enough must stay to feed every CTA
+  // through donations.
+  E->active_target = c.active_queries ? c.active_queries : SCS_DEFAULT_ACTIVE;
+  E->stats[SCS_STAT_ACTIVE] = E->active_target;
   E->pool.desc_cap = 1u << 24;
   RC(E->dalloc(&E->pool.desc, E->pool.desc_cap));
   RC(E->dalloc(&E->pool.head, 1));
@@ -372,6 +394,10 @@ static void finish_result(scs_engine *E, uint32_t si, uint32_t degree,
   d.r.latency_ns = now_ns() - sh.p.t_submit;
   E->done.push_back(std::move(d));
   sh.busy = false;
+  if (sh.parked) {  // a query whose preparation failed is never released
+    sh.parked = false;
+    E->n_parked--;
+  }
 }
 
 // Finish queries answered without a search (bad input, heuristic hit).
@@ -463,9 +489,15 @@ static int admit(scs_engine *E) {
     j.limit_doms = std::min<uint32_t>(p.q.limit_doms, MAX_DOMS);
     j.rules = E->rules;
     j.kl_heu = a.kl;
-    j.root_to_pool = 1;
+    j.root_to_pool = 2;  // parked; release_kernel publishes it
+    const unsigned long long roff = (unsigned long long)si * E->root_stride;
+    j.pad0 = (uint32_t)roff;
+    j.pad1 = (uint32_t)(roff >> 32);
     j.node_budget = E->cfg.node_budget;
     jobs.push_back(j);
+    sh.parked = true;
+    E->parked.push_back(si);
+    E->n_parked++;
   }
   if (jobs.empty()) return 0;
   cudaMemcpyAsync(E->d_jobs, jobs.data(), jobs.size() * sizeof(PrepJob),
@@ -485,6 +517,29 @@ static int admit(scs_engine *E) {
 // one search slice + collection of finished slots
 static int slice(scs_engine *E) {
   uint64_t t_us = E->cfg.slice_us ? E->cfg.slice_us : 20000;
+  // release parked roots up to the active target
+  {
+    const uint32_t active = E->running - std::min(E->running, E->n_parked);
+    std::vector<uint32_t> rel;
+    while (!E->parked.empty() && active + rel.size() < E->active_target) {
+      const uint32_t si = E->parked.front();
+      E->parked.pop_front();
+      if (!E->slots[si].parked) continue;  // collected already (preparation failed)
+      E->slots[si].parked = false;
+      E->n_parked--;
+      rel.push_back(si);
+    }
+    if (!rel.empty()) {
+      CK(cudaMemcpyAsync(E->d_rel, rel.data(), rel.size() * 4, cudaMemcpyHostToDevice,
+                         E->stream));
+      release_kernel<<<1, 32, 0, E->stream>>>(E->d_slots, E->d_rel, (uint32_t)rel.size(),
+                                              E->root_stride, E->pool, E->d_ctr);
+      CK(cudaGetLastError());
+      E->stats[SCS_STAT_LAUNCHES]++;
+      E->stats[SCS_STAT_RELEASES] += rel.size();
+      E->stats[SCS_STAT_H2D] += rel.size() * 4;
+    }
+  }
   SearchParams P = make_params(E);
   P.slice_ns = t_us * 1000ull;
   // per-slice fields: deadline (set by the first CTA), hungry, error,
@@ -543,7 +598,7 @@ static int slice(scs_engine *E) {
              std::to_string(hc.err_info[2]) + "," + std::to_string(hc.err_info[3]);
     fprintf(stderr, "scs: %s\n", E->err.c_str());
     if (hc.error & (ERR_RECORD | ERR_SPIN)) return SCS_ECUDA;
-    E->stats[SCS_STAT_COUNT - 1] |= hc.error;
+    E->stats[SCS_STAT_ERRORS] |= hc.error;
   }
   // collect finished slots
   for (uint32_t i = 0; i < E->nslots; i++) {
@@ -572,10 +627,12 @@ static int slice(scs_engine *E) {
   // pool reset when fully drained: every published record taken, and
   // something allocated (failed reservations also advance arena_top, so a
   // full arena with nothing published is reset too)
-  if (ph[0] >= std::min(ph[1], E->pool.desc_cap) && (ph[1] > 0 || arena_used > 0)) {
+  if (ph[0] >= std::min(ph[1], E->pool.desc_cap) && (ph[1] > 0 || arena_used > E->root_words)) {
     uint32_t used = std::min(ph[1], E->pool.desc_cap);
     CK(cudaMemsetAsync(E->pool.desc, 0, used * 8ull, E->stream));
-    CK(cudaMemsetAsync(E->pool.arena_top, 0, 8, E->stream));
+    // the bump area restarts after the parked roots, which stay in place
+    CK(cudaMemcpyAsync(E->pool.arena_top, &E->root_words, 8, cudaMemcpyHostToDevice,
+                       E->stream));
     CK(cudaMemsetAsync(E->pool.head, 0, 4, E->stream));
     CK(cudaMemsetAsync(E->pool.tail, 0, 4, E->stream));
   }

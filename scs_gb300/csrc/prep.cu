@@ -64,9 +64,16 @@ prep_kernel(DevGraph g, SlotArrays sa, Slot *slots, const PrepJob *jobs,
   }
   __syncthreads();
   const uint32_t len = 2 * nl + 5;
+  // root_to_pool 1: the root goes to the bump area and is published now;
+  // 2: it is parked at the slot's fixed offset (pad0/pad1) at the head of
+  // the arena and published later by release_kernel.
+  const bool parked = job.root_to_pool == 2;
   if (t == 0) {
     unsigned long long off = 0;
-    if (job.root_to_pool) off = atomicAdd(pool.arena_top, (unsigned long long)len);
+    if (parked)
+      off = (unsigned long long)job.pad0 | ((unsigned long long)job.pad1 << 32);
+    else if (job.root_to_pool)
+      off = atomicAdd(pool.arena_top, (unsigned long long)len);
     sh_root = off;
   }
   __syncthreads();
@@ -120,7 +127,7 @@ prep_kernel(DevGraph g, SlotArrays sa, Slot *slots, const PrepJob *jobs,
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
     sl->t_admit = now;
     if (job.root_to_pool) {
-      atomicAdd(&ctr->pending, 1ull);
+      if (!parked) atomicAdd(&ctr->pending, 1ull);  // a parked root counts when released
       atomicAdd(&ctr->prep_bytes, 8ull * nl + 20ull);
     } else {
       sl->pending = 0;
@@ -133,7 +140,7 @@ prep_kernel(DevGraph g, SlotArrays sa, Slot *slots, const PrepJob *jobs,
   __syncthreads();
   if (t == 0) {
     sl->state = SLOT_SEARCH;
-    if (job.root_to_pool) {
+    if (job.root_to_pool == 1) {
       uint32_t tk = atomicAdd(pool.tail, 1u);
       if (tk < pool.desc_cap) {
         __threadfence();
@@ -142,6 +149,31 @@ prep_kernel(DevGraph g, SlotArrays sa, Slot *slots, const PrepJob *jobs,
         atomicOr(&ctr->error, ERR_POOL);
       }
     }
+  }
+}
+
+// Publish the parked roots of the given slots (one thread; a few per
+// slice).  A slot whose preprocessing failed is already done and is skipped.
+// The query's task is counted before its descriptor becomes visible.
+__global__ void release_kernel(Slot *slots, const uint32_t *cand, uint32_t n,
+                               unsigned long long root_stride, Pool pool,
+                               Counters *ctr) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  for (uint32_t i = 0; i < n; i++) {
+    const uint32_t slot = cand[i];
+    Slot *sl = slots + slot;
+    if (*(volatile uint32_t *)&sl->state != SLOT_SEARCH) continue;
+    unsigned long long now;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
+    sl->t_admit = now;  // search time runs from activation
+    atomicAdd(&ctr->pending, 1ull);
+    const uint32_t tk = atomicAdd(pool.tail, 1u);
+    if (tk >= pool.desc_cap) {
+      atomicOr(&ctr->error, ERR_POOL);
+      continue;
+    }
+    __threadfence();
+    atomicExch(&pool.desc[tk], (unsigned long long)slot * root_stride + 1ull);
   }
 }
 

@@ -208,6 +208,9 @@ __global__ void prep_kernel(DevGraph g, SlotArrays sa, Slot *slots,
                             const PrepJob *jobs, int njobs, PrepScratch ps,
                             Pool pool, Counters *ctr);
 __global__ void search_kernel(SearchParams P);
+__global__ void release_kernel(Slot *slots, const uint32_t *cand, uint32_t n,
+                               unsigned long long root_stride, Pool pool,
+                               Counters *ctr);
 // core numbers of a device CSR by level-synchronous peeling (core.cu)
 int gpu_core_numbers(const uint32_t *d_off, const uint32_t *d_adj, uint32_t n,
                      uint32_t *d_core, uint32_t *d_scratch, void *ctr_dev,

@@ -23,7 +23,8 @@ STATUS_NAMES = {DONE: "done", HEURISTIC: "heuristic", CAPACITY: "capacity",
 
 STAT_NAMES = ["nodes", "slices", "donations", "steals", "spills", "bytes",
               "prep_bytes", "search_ns", "prep_ns", "launches", "h2d_bytes",
-              "d2h_bytes", "heur_ns", "ctas", "smem_words"]
+              "d2h_bytes", "heur_ns", "ctas", "smem_words", "errors", "active",
+              "releases"]
 
 
 class Config(C.Structure):
@@ -34,7 +35,7 @@ class Config(C.Structure):
                 ("threads_per_cta", C.c_uint32), ("stack_words", C.c_uint64),
                 ("pool_words", C.c_uint64), ("slice_us", C.c_uint32),
                 ("node_budget", C.c_uint64), ("host_threads", C.c_uint32),
-                ("device", C.c_int32)]
+                ("device", C.c_int32), ("active_queries", C.c_uint32)]
 
 
 class Query(C.Structure):
@@ -219,7 +220,7 @@ class Engine:
 
     def __init__(self, graph=None, csr=None, limit_queries=64, rules=None,
                  slice_us=20000, node_budget=0, ctas_per_sm=0, stack_words=0,
-                 pool_words=0, host_threads=0, device=0):
+                 pool_words=0, host_threads=0, device=0, active_queries=0):
         L = lib()
         cfg = Config()
         cfg.limit_queries = limit_queries
@@ -230,6 +231,7 @@ class Engine:
         cfg.pool_words = pool_words
         cfg.host_threads = host_threads
         cfg.device = device
+        cfg.active_queries = active_queries
         if rules is not None:
             cfg.rules_set = 1
             cfg.red1, cfg.red2, cfg.red3, cfg.prun1, cfg.prun2 = [int(bool(r)) for r in rules]
@@ -303,7 +305,7 @@ class Engine:
         return [got[t] for t in tickets]
 
     def stats(self):
-        arr = (C.c_uint64 * 16)()
+        arr = (C.c_uint64 * 20)()
         self._check(lib().scs_stats(self._h, arr), "scs_stats")
         return {name: int(arr[i]) for i, name in enumerate(STAT_NAMES)}
 

@@ -214,3 +214,25 @@ def test_default_occupancy_three_ctas_per_sm(rmat15):
         assert st["smem_words"] > 16000, st
     finally:
         e.close()
+
+
+def test_active_target_releases_every_query_and_answers_match(chunglu_small, og_c1):
+    """Queries are prepared together and released to the search a few at a
+    time (scs_config.active_queries).  With two active at once the answers
+    still equal the oracle's, and every searched query is released exactly
+    once."""
+    gold = [g for g in _golden_c1()["queries"] if g["finished"]][:16]
+    rows = [(g["l"], g["h"], g["q"], g["heur"], g["limit_doms"]) for g in gold]
+    e = _engine(graph=chunglu_small, limit_queries=32, active_queries=2)
+    try:
+        res = e.solve(rows)
+        st = e.stats()
+    finally:
+        e.close()
+    assert st["active"] == 2
+    searched = 0
+    for g, r in zip(gold, res):
+        assert r["status"] in (0, 1), r
+        assert r["degree"] == g["degree"], (g, r)
+        searched += r["nodes"] > 0
+    assert st["releases"] == searched
