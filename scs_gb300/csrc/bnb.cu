@@ -61,6 +61,11 @@ static_assert(SCS_LANE_DOM % 8 == 0, "stage 1 checks whole 8-word groups");
 #ifndef SCS_ROW_UNROLL
 #define SCS_ROW_UNROLL 8
 #endif
+// ustar argmax pass: candidates per thread whose loads are issued together
+// (2 measured 0.5 % above 1 on the bench; 4 adds spills and loses it)
+#ifndef SCS_ARGMAX_UNROLL
+#define SCS_ARGMAX_UNROLL 2
+#endif
 constexpr int NWARP = BT / 32;
 
 // What the four sub-phase counters of scs_profile measure (they cost a few
@@ -1119,27 +1124,47 @@ __device__ void choose_ustar(Task &T, Sh &sh) {
   const double dmax = (double)sh.dmax;
   double best = 0.0;
   uint32_t bid = UINT32_MAX, bpos = 0;
-  for (uint32_t ci = t; ci < nc; ci += BT) {
-    const uint32_t pk = T.tmp[ci], x = pk & 0xFFFFu;
-    double sc;
-    if (masked) {
-      unsigned long long m = reinterpret_cast<const unsigned long long *>(T.ssc)[x];
-      T.cmask[x] = m;  // kept for the dominance prefilter
-      sc = 0.0;
-      while (m) {
-        const int r = __ffsll((long long)m) - 1;
-        m &= m - 1;
-        sc = __dadd_rn(sc, sh.wtab[r]);
-      }
-      T.ssc[x] = sc;  // the mask word becomes the pushed score
-    } else {
-      sc = T.ssc[x];
+  // SCS_ARGMAX_UNROLL candidates per thread at a time: their packed ids, then
+  // their masks (or scores) and state words, are loaded together
+  for (uint32_t c0 = 0; c0 < nc; c0 += BT * SCS_ARGMAX_UNROLL) {
+    uint32_t pk[SCS_ARGMAX_UNROLL];
+#pragma unroll
+    for (int j = 0; j < SCS_ARGMAX_UNROLL; j++) {
+      const uint32_t ci = c0 + BT * j + t;
+      pk[j] = ci < nc ? T.tmp[ci] : SENT;
     }
-    if (sc > 0.0) sc = __dadd_rn(sc, __ddiv_rn((double)dr_of(T.W[x]), dmax));
-    if (sc > best || (sc == best && sc > 0.0 && x < bid)) {
-      best = sc;
-      bid = x;
-      bpos = pk >> 16;
+    unsigned long long mv[SCS_ARGMAX_UNROLL];
+    uint32_t wv[SCS_ARGMAX_UNROLL];
+#pragma unroll
+    for (int j = 0; j < SCS_ARGMAX_UNROLL; j++) {
+      const uint32_t x = pk[j] != SENT ? (pk[j] & 0xFFFFu) : 0u;
+      mv[j] = reinterpret_cast<const unsigned long long *>(T.ssc)[x];
+      wv[j] = T.W[x];
+    }
+#pragma unroll
+    for (int j = 0; j < SCS_ARGMAX_UNROLL; j++) {
+      if (pk[j] == SENT) continue;
+      const uint32_t x = pk[j] & 0xFFFFu;
+      double sc;
+      if (masked) {
+        unsigned long long m = mv[j];
+        T.cmask[x] = m;  // kept for the dominance prefilter
+        sc = 0.0;
+        while (m) {
+          const int r = __ffsll((long long)m) - 1;
+          m &= m - 1;
+          sc = __dadd_rn(sc, sh.wtab[r]);
+        }
+        T.ssc[x] = sc;  // the mask word becomes the pushed score
+      } else {
+        sc = __longlong_as_double((long long)mv[j]);
+      }
+      if (sc > 0.0) sc = __dadd_rn(sc, __ddiv_rn((double)dr_of(wv[j]), dmax));
+      if (sc > best || (sc == best && sc > 0.0 && x < bid)) {
+        best = sc;
+        bid = x;
+        bpos = pk[j] >> 16;
+      }
     }
   }
   double osc;
@@ -1358,7 +1383,7 @@ __device__ __forceinline__ void child_entry(uint32_t x, uint32_t w, uint32_t a,
 }
 
 __device__ void mark_children(Task &T, Sh &sh) {
-  const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+  const int t = threadIdx.x, wid = t >> 5;
   const uint32_t k = sh.ndoms;
   // adjacency bits: warp per marked vertex
   for (uint32_t j = wid; j <= k; j += NWARP) {
@@ -1487,7 +1512,7 @@ __device__ void write_children(Task &T, Sh &sh, uint32_t code_lo,
 
 // apply the Include child to the in-CTA state (continue depth-first)
 __device__ void apply_include(Task &T, Sh &sh) {
-  const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+  const int t = threadIdx.x;
   const uint32_t s = sh.s, k = sh.ndoms;
   for (uint32_t i = t; i < s; i += BT) {
     uint32_t x = T.list[i];
