@@ -240,7 +240,7 @@ def main():
     from scs_gb300.engine import core_numbers
     core = core_numbers(n, off, adj)
     warm = queries_for(core, args.warmup_batch * args.warmup, 43 + 1000 * rank)
-    tune = {"ctas_per_sm": args.ctas_per_sm, "slice_us": args.slice_us or 20000}
+    tune = {"ctas_per_sm": args.ctas_per_sm, "slice_us": args.slice_us or 80000}
     if not args.ctas_per_sm:
         # launch shape chosen by the autotuner on warm-up queries (not timed)
         from scs_gb300.autotune import autotune

@@ -60,7 +60,8 @@ typedef struct {
   uint32_t threads_per_cta;   /* 256 or 512 (0: auto)                    */
   uint64_t stack_words;       /* task-stack words per CTA (0: auto)      */
   uint64_t pool_words;        /* shared task-pool words (0: auto)        */
-  uint32_t slice_us;          /* search time slice in microseconds       */
+  uint32_t slice_us;          /* search time slice in microseconds (0: 80 ms;
+                                 new queries are admitted between slices) */
   uint64_t node_budget;       /* per-query task budget, 0 = unlimited
                                  (stands in for the level cap main.cu:444) */
   uint32_t host_threads;      /* threads for the greedy incumbent (0: auto) */

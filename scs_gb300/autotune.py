@@ -21,7 +21,7 @@ import time
 import numpy as np
 
 CACHE_DIR = os.environ.get("SCS_TUNE_DIR", os.path.join(os.path.expanduser("~"), ".cache", "scs_gb300"))
-DEFAULT_GRID = [(3, 20000), (2, 20000)]
+DEFAULT_GRID = [(3, 80000), (2, 80000)]
 
 
 def graph_key(off, adj, rows):

@@ -71,6 +71,11 @@ std::string g_create_error;
 
 // Queries searched at once unless scs_config.active_queries says otherwise.
 constexpr uint32_t SCS_DEFAULT_ACTIVE = 32;
+// Search slice length unless scs_config.slice_us says otherwise.  A slice
+// ends early when no work is left; a longer one spends less of its time on
+// the CTAs that finish their last step after the deadline (bench: 20 ms
+// 61.3 queries/s, 40 ms 62.7, 80 ms 63.4), but admits new queries later.
+constexpr uint64_t SCS_DEFAULT_SLICE_US = 80000;
 
 }  // namespace
 
@@ -516,7 +521,7 @@ static int admit(scs_engine *E) {
 
 // one search slice + collection of finished slots
 static int slice(scs_engine *E) {
-  uint64_t t_us = E->cfg.slice_us ? E->cfg.slice_us : 20000;
+  uint64_t t_us = E->cfg.slice_us ? E->cfg.slice_us : SCS_DEFAULT_SLICE_US;
   // release parked roots up to the active target
   {
     const uint32_t active = E->running - std::min(E->running, E->n_parked);

@@ -219,7 +219,7 @@ class Engine:
     query slots (limit_queries), rule switches red1..prun2."""
 
     def __init__(self, graph=None, csr=None, limit_queries=64, rules=None,
-                 slice_us=20000, node_budget=0, ctas_per_sm=0, stack_words=0,
+                 slice_us=0, node_budget=0, ctas_per_sm=0, stack_words=0,
                  pool_words=0, host_threads=0, device=0, active_queries=0):
         L = lib()
         cfg = Config()
