@@ -200,6 +200,13 @@ int scs_greedy_incumbent(uint32_t n, const uint32_t *off, const uint32_t *adj,
 /* Distance bound ubD from n(k, D) (main.cu:154-172). */
 uint32_t scs_distance_bound(uint32_t kl, uint32_t h);
 
+/* Layout of the public structs as compiled, for bindings to check theirs:
+ * out[0..7] = sizeof(scs_config), offsetof(scs_config, node_budget),
+ * offsetof(scs_config, device), offsetof(scs_config, active_queries),
+ * sizeof(scs_query), sizeof(scs_result), offsetof(scs_result, nodes),
+ * offsetof(scs_result, search_ns).  Returns the count written (<= max). */
+int scs_abi_layout(uint64_t *out, int max);
+
 /* Check an answer community H[0..hs) of query (l, h, q) against a CSR graph
  * (the checks the reference's results imply but never perform: it reports
  * only the degree, main.cu:328-334).  Returns SCS_CHECK_OK when every id is

@@ -1,5 +1,6 @@
 // host_api.cpp -- host-only entry points of include/scs.h (no GPU needed).
 #include <algorithm>
+#include <cstddef>
 #include <cstdlib>
 #include <cstring>
 #include <string>
@@ -100,6 +101,17 @@ int scs_greedy_incumbent(uint32_t n, const uint32_t *off, const uint32_t *adj,
 }
 
 uint32_t scs_distance_bound(uint32_t kl, uint32_t h) { return ubd_host(kl, h); }
+
+int scs_abi_layout(uint64_t *out, int max) {
+  if (!out || max < 0) return SCS_EINVAL;
+  const uint64_t v[8] = {sizeof(scs_config),        offsetof(scs_config, node_budget),
+                         offsetof(scs_config, device), offsetof(scs_config, active_queries),
+                         sizeof(scs_query),         sizeof(scs_result),
+                         offsetof(scs_result, nodes), offsetof(scs_result, search_ns)};
+  const int n = max < 8 ? max : 8;
+  for (int i = 0; i < n; i++) out[i] = v[i];
+  return n;
+}
 
 }  // extern "C"
 

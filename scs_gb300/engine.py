@@ -92,6 +92,7 @@ def lib(build_if_missing=False):
                                        C.c_uint32, _u32p, _u32p, _u32p]
     L.scs_distance_bound.argtypes = [C.c_uint32, C.c_uint32]
     L.scs_distance_bound.restype = C.c_uint32
+    L.scs_abi_layout.argtypes = [_u64p, C.c_int]
     L.scs_check_community.argtypes = [C.c_uint32, _u32p, _u32p, _u32p, C.c_uint32, C.c_uint32,
                                       C.c_uint32, C.c_uint32, _u32p]
     L.scs_local_graph_noalloc.argtypes = [vp, vp, vp, C.c_uint32, C.c_uint32, C.c_uint32,

@@ -193,3 +193,19 @@ print(n)
         out = subprocess.run([sys.executable, "-c", code, os.path.join(REF, graph),
                               os.path.join(REF, qf)], capture_output=True, text=True)
         assert out.returncode == 0, out.stderr[-2000:]
+
+
+def test_binding_structs_match_the_compiled_abi():
+    """The ctypes mirrors of scs_config / scs_query / scs_result have the
+    sizes and field offsets the library was compiled with."""
+    import ctypes as C
+    import numpy as np
+    from scs_gb300 import build as B
+    from scs_gb300 import engine as E
+    B.build()
+    out = np.zeros(8, dtype=np.uint64)
+    assert E.lib().scs_abi_layout(out.ctypes.data_as(C.POINTER(C.c_uint64)), 8) == 8
+    want = [C.sizeof(E.Config), E.Config.node_budget.offset, E.Config.device.offset,
+            E.Config.active_queries.offset, C.sizeof(E.Query), C.sizeof(E.Result),
+            E.Result.nodes.offset, E.Result.search_ns.offset]
+    assert out.tolist() == want
