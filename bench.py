@@ -205,6 +205,65 @@ def run_reference(args):
     return 0
 
 
+def run_serve(args):
+    """Serving mode: queries arrive as a Poisson process at each rate for
+    --serve-seconds and are submitted at their arrival times while the engine
+    steps (admission between slices, 5 ms slices unless --slice-us says
+    otherwise).  Latency runs from arrival to the result; throughput is the
+    completed queries over the time to the last result.  One GPU, rank 0."""
+    rank, world, local = env_rank()
+    if rank != 0:
+        return 0
+    from scs_gb300.engine import Engine, core_numbers
+    n, off, adj = build_workload(args.batch, args.warmup, args.steps)
+    core = core_numbers(n, off, adj)
+    for rate in [float(x) for x in args.serve.split(",") if x]:
+        count = max(1, int(rate * args.serve_seconds))
+        rows = [tuple(int(x) for x in r) for r in queries_for(core, count, 44)]
+        rng = np.random.default_rng(45)
+        arrive = np.cumsum(rng.exponential(1.0 / rate, count))
+        eng = Engine(csr=(n, off, adj), limit_queries=256, slice_us=args.slice_us or 5000,
+                     ctas_per_sm=args.ctas_per_sm, node_budget=args.node_budget,
+                     stack_words=args.stack_words, pool_words=args.pool_words, device=local,
+                     active_queries=args.active_queries)
+        eng.solve([tuple(int(x) for x in r) for r in queries_for(core, 8, 46)])  # warm-up
+        pending, lat, res = {}, [], []
+        i = 0
+        t0 = time.perf_counter()
+        cap = args.serve_seconds * 20 + 60
+        while len(res) < count:
+            now = time.perf_counter() - t0
+            if now > cap:
+                break
+            while i < count and arrive[i] <= now:
+                pending[eng.submit(*rows[i])] = (arrive[i], now)
+                i += 1
+            busy = eng.step()
+            for r in eng.poll():
+                a, s = pending.pop(r["ticket"])
+                lat.append((s - a) + r["latency_ns"] / 1e9)
+                res.append(r)
+            if not busy and i < count:
+                time.sleep(max(0.0, min(arrive[i] - (time.perf_counter() - t0), 0.002)))
+        span = time.perf_counter() - t0
+        st = eng.stats()
+        eng.close()
+        lat_ms = np.array(lat) * 1e3 if lat else np.zeros(1)
+        line = {"mode": "serve", "metric": METRIC, "unit": UNIT, "n_gpus": 1,
+                "offered_qps": rate, "arrivals": count, "completed": len(res),
+                "throughput_qps": len(res) / span if span > 0 else None,
+                "p50_ms": float(np.percentile(lat_ms, 50)),
+                "p99_ms": float(np.percentile(lat_ms, 99)),
+                "exact_fraction": sum(1 for r in res if r["status"] in (0, 1)) / max(len(res), 1),
+                "verified_fraction": sum(1 for r in res if r["h_verified"]) / max(len(res), 1),
+                "data": "synthetic",
+                "config": {"workload": WORKLOAD, "arrival_window_s": args.serve_seconds,
+                           "node_budget": args.node_budget, "slice_us": args.slice_us or 5000,
+                           "active_queries": st["active"], "slots": 256}}
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -225,9 +284,16 @@ def main():
     ap.add_argument("--stack-words", type=int, default=0,
                     help="task-stack words per CTA (0: sized from device memory)")
     ap.add_argument("--pool-words", type=int, default=0)
+    ap.add_argument("--serve", default="",
+                    help="serving mode: Poisson arrival rates in queries/s, comma-separated "
+                         "(one JSON line per rate, latency measured from arrival)")
+    ap.add_argument("--serve-seconds", type=float, default=20.0,
+                    help="serving mode: arrival window per rate (seconds)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.serve:
+        return run_serve(args)
 
     import torch
     rank, world, local = env_rank()
