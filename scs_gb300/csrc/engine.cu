@@ -4,8 +4,9 @@
 //   submit -> admission into a free slot: ku = min(core[q], h-1)
 //   (inc/Intialize.h:207), greedy incumbent on host threads
 //   (inc/heuristic.h:321-349), early answer when kl == ku (main.cu:122-133),
-//   ubD (main.cu:154-172) -> preprocessing kernel (prep.cu) -> the root task
-//   enters the shared pool -> time-sliced persistent search (bnb.cu) until
+//   ubD (main.cu:154-172) -> preprocessing kernel (prep.cu), root task parked
+//   -> released to the shared pool while fewer than active_queries queries
+//   are searched -> time-sliced persistent search (bnb.cu) until
 //   the query's outstanding-task count reaches zero -> result.
 // Unlike the reference, admission happens between search slices while other
 // queries keep their tasks on the device (continuous batching), the level
@@ -496,8 +497,8 @@ static int admit(scs_engine *E) {
     j.kl_heu = a.kl;
     j.root_to_pool = 2;  // parked; release_kernel publishes it
     const unsigned long long roff = (unsigned long long)si * E->root_stride;
-    j.pad0 = (uint32_t)roff;
-    j.pad1 = (uint32_t)(roff >> 32);
+    j.root_off_lo = (uint32_t)roff;
+    j.root_off_hi = (uint32_t)(roff >> 32);
     j.node_budget = E->cfg.node_budget;
     jobs.push_back(j);
     sh.parked = true;

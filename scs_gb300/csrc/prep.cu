@@ -65,13 +65,13 @@ prep_kernel(DevGraph g, SlotArrays sa, Slot *slots, const PrepJob *jobs,
   __syncthreads();
   const uint32_t len = 2 * nl + 5;
   // root_to_pool 1: the root goes to the bump area and is published now;
-  // 2: it is parked at the slot's fixed offset (pad0/pad1) at the head of
+  // 2: it is parked at the slot's fixed offset (root_off_lo/hi) at the head of
   // the arena and published later by release_kernel.
   const bool parked = job.root_to_pool == 2;
   if (t == 0) {
     unsigned long long off = 0;
     if (parked)
-      off = (unsigned long long)job.pad0 | ((unsigned long long)job.pad1 << 32);
+      off = (unsigned long long)job.root_off_lo | ((unsigned long long)job.root_off_hi << 32);
     else if (job.root_to_pool)
       off = atomicAdd(pool.arena_top, (unsigned long long)len);
     sh_root = off;

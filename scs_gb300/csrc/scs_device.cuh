@@ -152,7 +152,9 @@ __host__ __device__ inline uint32_t ubd_dev(uint32_t kl, uint32_t h) {
 struct PrepJob {
   uint32_t slot, q, kl, ubd;
   uint32_t l, h, limit_doms, rules;
-  uint32_t kl_heu, root_to_pool, pad0, pad1;
+  uint32_t kl_heu;
+  uint32_t root_to_pool;  // 0: no root; 1: root published now; 2: root parked
+  uint32_t root_off_lo, root_off_hi;  // parked root's arena offset (words)
   unsigned long long node_budget;
 };
 
