@@ -281,6 +281,8 @@ def main():
     ap.add_argument("--slice-us", type=int, default=0)
     ap.add_argument("--active-queries", type=int, default=0,
                     help="queries searched at once (0: the engine default)")
+    ap.add_argument("--release-order", type=int, default=0,
+                    help="next prepared query to search: 0 smallest local graph, 1 admission order")
     ap.add_argument("--stack-words", type=int, default=0,
                     help="task-stack words per CTA (0: sized from device memory)")
     ap.add_argument("--pool-words", type=int, default=0)
@@ -318,7 +320,7 @@ def main():
                  slice_us=tune["slice_us"], ctas_per_sm=tune["ctas_per_sm"],
                  node_budget=args.node_budget, stack_words=args.stack_words,
                  pool_words=args.pool_words, device=local,
-                 active_queries=args.active_queries)
+                 active_queries=args.active_queries, release_order=args.release_order)
     # weak scaling: every rank runs the full 1,000-query workload of its own
     # query seed (rank 0 uses the workload's seed 42)
     rows = queries_for(core, args.batch * args.steps, 42 + 1000 * rank)

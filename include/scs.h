@@ -69,6 +69,9 @@ typedef struct {
   uint32_t active_queries;    /* queries searched at once; the other admitted
                                  ones wait prepared (0: auto, 32). Fewer keep
                                  the searched local graphs in L2. */
+  uint32_t release_order;     /* which prepared query is searched next:
+                                 0 the smallest local graph (shortest job
+                                 first), 1 admission order */
 } scs_config;
 
 /* One query: the reference's message fields (main.cu:92-119). */

@@ -502,6 +502,7 @@ static int admit(scs_engine *E) {
     j.node_budget = E->cfg.node_budget;
     jobs.push_back(j);
     sh.parked = true;
+    E->h_slots[si].n_local = 0;  // unknown until the next read-back
     E->parked.push_back(si);
     E->n_parked++;
   }
@@ -526,14 +527,31 @@ static int slice(scs_engine *E) {
   // release parked roots up to the active target
   {
     const uint32_t active = E->running - std::min(E->running, E->n_parked);
+    const uint32_t need = E->active_target > active ? E->active_target - active : 0;
     std::vector<uint32_t> rel;
-    while (!E->parked.empty() && active + rel.size() < E->active_target) {
-      const uint32_t si = E->parked.front();
-      E->parked.pop_front();
-      if (!E->slots[si].parked) continue;  // collected already (preparation failed)
-      E->slots[si].parked = false;
-      E->n_parked--;
-      rel.push_back(si);
+    if (need && E->n_parked) {
+      // candidates in admission order (entries of collected slots dropped)
+      std::vector<uint32_t> cand;
+      cand.reserve(E->parked.size());
+      for (uint32_t si : E->parked)
+        if (E->slots[si].parked) cand.push_back(si);
+      if (E->cfg.release_order == 0 && cand.size() > need) {
+        // shortest job first: the smallest local graphs, as read back after
+        // the slice that followed their preparation (0 until then, so a
+        // just-prepared query is not held back); ties keep admission order
+        std::stable_sort(cand.begin(), cand.end(), [&](uint32_t a, uint32_t b) {
+          return E->h_slots[a].n_local < E->h_slots[b].n_local;
+        });
+      }
+      for (uint32_t i = 0; i < cand.size() && rel.size() < need; i++) {
+        E->slots[cand[i]].parked = false;
+        E->n_parked--;
+        rel.push_back(cand[i]);
+      }
+      std::deque<uint32_t> keep;
+      for (uint32_t si : E->parked)
+        if (E->slots[si].parked) keep.push_back(si);
+      E->parked.swap(keep);
     }
     if (!rel.empty()) {
       CK(cudaMemcpyAsync(E->d_rel, rel.data(), rel.size() * 4, cudaMemcpyHostToDevice,
