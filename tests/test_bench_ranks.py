@@ -42,3 +42,24 @@ def test_replica_timing_reduction_two_ranks():
         assert p.exitcode == 0
     for rank, t_dev, wall, n in out:
         assert t_dev == 2.0 and wall == 5.0 and n == 2000
+
+
+def test_reference_arm_prints_the_contract_line():
+    """`bench.py --impl reference` (the CPU port on the host cores) prints one
+    JSON line with the arm's keys; a small bounded sample keeps it short."""
+    import json
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--steps", "1",
+                        "--warmup", "0", "--batch", "4", "--cpu-cap", "1"],
+                       cwd=root, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference"
+    for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step",
+              "higher_is_better", "cpu_baseline", "e2e", "config"):
+        assert k in line, k
+    assert line["value"] > 0
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
