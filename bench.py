@@ -15,12 +15,15 @@ reference's level cap, main.cu:444-463); a query that hits it reports the
 best degree found with status "timeout" (the reference's Overtime=1) and
 does not count as exact.
 
-value  = queries / device time of the timed steps (CUDA events, graph
-         resident, queries already submitted);
-e2e    = queries / time of the same steps through the C ABI from host
-         buffers (submit, run, poll of results and communities).
+value  = queries / device time of the timed steps (CUDA events on the
+         engine's stream around submit, run and poll; graph resident);
+e2e    = queries / host-clock time of the same calls through the C ABI from
+         host buffers (submit, run, poll of results and communities).  The
+         engine is host-driven between slices, so the two agree.
 --impl reference times the reference's CPU path (the oracle port of its
 branch-and-bound on the reference's heuristics) on the host cores.
+--serve RATES runs Poisson arrivals at each rate (queries/s) instead and
+prints one line per rate with latency from arrival (see run_serve).
 """
 import argparse
 import json
