@@ -119,9 +119,11 @@ int scs_core_numbers(scs_engine *e, uint32_t *core_out);
  * scs_run/scs_step as slots free up (continuous batching). */
 int scs_submit(scs_engine *e, const scs_query *q, uint64_t *ticket);
 
-/* Advance the engine: admit waiting queries into free slots, run one search
- * slice, collect finished queries.  Returns the number of queries still
- * outstanding (queued + running), or a negative error. */
+/* Advance the engine: admit waiting queries into free slots (prepared on the
+ * device together), release prepared queries to the search up to
+ * active_queries, run one search slice, collect finished queries.  Returns
+ * the number of queries still outstanding (queued + admitted), or a negative
+ * error. */
 int scs_step(scs_engine *e);
 
 /* Run until every submitted query has a result. */
