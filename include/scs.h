@@ -17,8 +17,10 @@
  *   scs_destroy                  <- main.cu:586-594 (free + device reset).
  *
  * Conventions: every call returns 0 or a negative SCS_E* code; nothing calls
- * exit().  Plain pointers and sizes only.  One engine drives one GPU; calls on
- * one engine must come from one thread at a time.
+ * exit().  Plain pointers and sizes only.  One engine drives one GPU.
+ * scs_submit may be called from any number of threads, also while another
+ * thread steps the engine; every other call on one engine must come from one
+ * thread at a time (the one that steps it).
  */
 #ifndef SCS_H
 #define SCS_H

@@ -724,26 +724,29 @@ int scs_core_numbers(scs_engine *E, uint32_t *core) {
 
 int scs_submit(scs_engine *E, const scs_query *q, uint64_t *ticket) {
   if (!E || !q) return SCS_EINVAL;
+  // May run on any thread while another one steps the engine: the ticket,
+  // the admission queue and the workers' queue change under heu_mu, which
+  // admission holds while it walks the queue.
   auto j = std::make_shared<Job>();
   j->p.q = *q;
-  j->p.ticket = E->next_ticket++;
   j->p.t_submit = now_ns();
-  if (q->q >= E->g.n || q->h < 1 || q->h >= CL_CAP - 1 || q->l > q->h) {
+  const bool bad = q->q >= E->g.n || q->h < 1 || q->h >= CL_CAP - 1 || q->l > q->h;
+  bool work = false;
+  if (bad) {
     j->bad = true;
     j->done = true;
   } else {
     j->ku = std::min(E->g.core[q->q], q->h - 1);
-    if (!q->heuristic) {
-      j->done = true;  // kl = 0
-    } else {
-      {
-        std::lock_guard<std::mutex> lk(E->heu_mu);
-        E->heu_todo.push_back(j);
-      }
-      E->heu_cv.notify_one();
-    }
+    if (!q->heuristic) j->done = true;  // kl = 0
+    else work = true;
   }
-  E->queue.push_back(j);
+  {
+    std::lock_guard<std::mutex> lk(E->heu_mu);
+    j->p.ticket = E->next_ticket++;
+    if (work) E->heu_todo.push_back(j);
+    E->queue.push_back(j);
+  }
+  if (work) E->heu_cv.notify_one();
   if (ticket) *ticket = j->p.ticket;
   return 0;
 }
@@ -753,7 +756,12 @@ int scs_step(scs_engine *E) {
   int a = admit(E);
   if (a < 0) return a;
   if (E->running > 0) RC(slice(E));
-  return (int)(E->queue.size() + E->running);
+  size_t queued;
+  {
+    std::lock_guard<std::mutex> lk(E->heu_mu);
+    queued = E->queue.size();
+  }
+  return (int)(queued + E->running);
 }
 
 int scs_run(scs_engine *E) {

@@ -236,3 +236,38 @@ def test_active_target_releases_every_query_and_answers_match(chunglu_small, og_
         assert r["degree"] == g["degree"], (g, r)
         searched += r["nodes"] > 0
     assert st["releases"] == searched
+
+
+def test_submit_from_many_threads_while_stepping(chunglu_small):
+    """scs_submit is safe from several threads while another thread steps
+    the engine: every query gets a distinct ticket and its exact answer."""
+    import threading
+    import time
+    gold = [g for g in _golden_c1()["queries"] if g["finished"]][:24]
+    rows = [(g["l"], g["h"], g["q"], g["heur"], g["limit_doms"]) for g in gold]
+    e = _engine(graph=chunglu_small, limit_queries=16)
+    tickets = {}
+
+    def submitter(k):
+        for i in range(k, len(rows), 4):
+            tickets[e.submit(*rows[i])] = i
+
+    ths = [threading.Thread(target=submitter, args=(k,)) for k in range(4)]
+    try:
+        for th in ths:
+            th.start()
+        got = {}
+        deadline = time.time() + 300
+        while len(got) < len(rows) and time.time() < deadline:
+            e.step()
+            for r in e.poll():
+                got[r["ticket"]] = r
+        for th in ths:
+            th.join()
+    finally:
+        e.close()
+    assert len(tickets) == len(rows) and len(got) == len(rows)
+    for t, r in got.items():
+        g = gold[tickets[t]]
+        assert r["status"] in (0, 1), r
+        assert r["degree"] == g["degree"], (g, r)
