@@ -289,6 +289,8 @@ def main():
     ap.add_argument("--stack-words", type=int, default=0,
                     help="task-stack words per CTA (0: sized from device memory)")
     ap.add_argument("--pool-words", type=int, default=0)
+    ap.add_argument("--clocks-csv", default="/tmp/scs_clocks_r%d.csv",
+                    help="where the nvidia-smi clock samples of the timed region go (%%d: rank)")
     ap.add_argument("--serve", default="",
                     help="serving mode: Poisson arrival rates in queries/s, comma-separated "
                          "(one JSON line per rate, latency measured from arrival)")
@@ -338,8 +340,7 @@ def main():
     for i in range(args.warmup):
         eng.solve([tuple(int(x) for x in r) for r in warm[i * wb:(i + 1) * wb]])
     st0 = eng.stats()
-    clocks = Clocks(os.path.join(ROOT, "gpurun_out", "clocks_r%d.csv" % rank)
-                    if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "/tmp/scs_clocks_%d.csv" % rank)
+    clocks = Clocks(args.clocks_csv % rank if "%d" in args.clocks_csv else args.clocks_csv)
     results, dev_ms, wall = [], 0.0, 0.0
     h2d = d2h = 0
     barrier()
