@@ -30,6 +30,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import threading
 import time
 
@@ -289,7 +290,7 @@ def main():
     ap.add_argument("--stack-words", type=int, default=0,
                     help="task-stack words per CTA (0: sized from device memory)")
     ap.add_argument("--pool-words", type=int, default=0)
-    ap.add_argument("--clocks-csv", default="/tmp/scs_clocks_r%d.csv",
+    ap.add_argument("--clocks-csv", default=os.path.join(tempfile.gettempdir(), "scs_clocks_r%d.csv"),
                     help="where the nvidia-smi clock samples of the timed region go (%%d: rank)")
     ap.add_argument("--serve", default="",
                     help="serving mode: Poisson arrival rates in queries/s, comma-separated "
