@@ -70,3 +70,23 @@ def test_engine_core_numbers_come_from_gpu_and_match_host(rmat15):
         assert np.array_equal(eng.core_numbers(), E.core_numbers(n, off, adj))
     finally:
         eng.close()
+
+
+@pytest.mark.parametrize("name,n,edges", list(_shapes()), ids=[s[0] for s in _shapes()])
+def test_host_core_matches_oracle_small(name, n, edges, oracle_lib):
+    """The host peeling (the GPU's reference above) equals the oracle's core
+    numbers, which are pinned to the reference's own loader and peeling."""
+    B.build()
+    off, adj = _csr(n, edges)
+    og = oracle_lib.OracleGraph(n, off, adj)
+    assert np.array_equal(E.core_numbers(n, off, adj), np.asarray(og.core, dtype=np.uint32))
+
+
+@pytest.mark.parametrize("gen", ["chunglu_n4000", "rmat_s15_ef16"])
+def test_host_core_matches_oracle_workloads(gen, oracle_lib):
+    B.build()
+    make, _ = W.WORKLOADS[gen]
+    n, u, v = make()
+    off, adj = W.to_csr(n, u, v)
+    og = oracle_lib.OracleGraph(n, off, adj)
+    assert np.array_equal(E.core_numbers(n, off, adj), np.asarray(og.core, dtype=np.uint32))
