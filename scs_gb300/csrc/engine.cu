@@ -507,14 +507,15 @@ static int admit(scs_engine *E) {
     E->n_parked++;
   }
   if (jobs.empty()) return 0;
-  cudaMemcpyAsync(E->d_jobs, jobs.data(), jobs.size() * sizeof(PrepJob),
-                  cudaMemcpyHostToDevice, E->stream);
+  CK(cudaMemcpyAsync(E->d_jobs, jobs.data(), jobs.size() * sizeof(PrepJob),
+                     cudaMemcpyHostToDevice, E->stream));
   E->stats[SCS_STAT_H2D] += jobs.size() * sizeof(PrepJob);
-  cudaEventRecord(E->ev2, E->stream);
+  CK(cudaEventRecord(E->ev2, E->stream));
   prep_kernel<<<(unsigned)jobs.size(), PREP_THREADS, 0, E->stream>>>(
       DevGraph{E->g.n, E->g.dmax, E->d_off, E->d_adj, E->d_core}, E->sa, E->d_slots,
       E->d_jobs, (int)jobs.size(), E->ps, E->pool, E->d_ctr);
-  cudaEventRecord(E->ev3, E->stream);
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(E->ev3, E->stream));
   E->prep_pending = true;
   E->stats[SCS_STAT_LAUNCHES]++;
   E->running += (uint32_t)jobs.size();
