@@ -15,13 +15,17 @@ reference's level cap, main.cu:444-463); a query that hits it reports the
 best degree found with status "timeout" (the reference's Overtime=1) and
 does not count as exact.
 
-value  = queries / device time of the timed steps (CUDA events on the
-         engine's stream around submit, run and poll; graph resident);
-e2e    = queries / host-clock time of the same calls through the C ABI from
-         host buffers (submit, run, poll of results and communities).  The
-         engine is host-driven between slices, so the two agree.
+value  = exact answers (status done or heuristic) / device time of the
+         timed steps (CUDA events on the engine's stream around submit, run
+         and poll; graph resident).  Budget-stopped answers are not counted;
+         all answers per second are reported beside it in config.
+e2e    = exact answers / host-clock time of the same calls through the C
+         ABI from host buffers (submit, run, poll of results and
+         communities).  The engine is host-driven between slices, so the two
+         agree.
 --impl reference times the reference's CPU path (the oracle port of its
-branch-and-bound on the reference's heuristics) on the host cores.
+branch-and-bound on the reference's heuristics) on all host cores, on a
+sample of each step's queries under the same node budget, no wall cap.
 --serve RATES runs Poisson arrivals at each rate (queries/s) instead and
 prints one line per rate with latency from arrival (see run_serve).
 """
@@ -137,26 +141,52 @@ def measured_peak_gbs():
     return 6800.0, "fallback"
 
 
-def cpu_baseline(n, off, adj, rows, budget, cap_s=10.0, procs=None):
-    """The CPU port (the reference's heuristics + its branch-and-bound rules,
-    oracle.c) on the host cores: one sampled query per process, same node
-    budget as the GPU plus a wall-clock cap per query.  Returns (qps, cores,
-    description).  Throughput = cores / mean per-query time; a capped query
-    counts with its capped time, which can only favour the CPU."""
+def host_cpu_info():
+    """Host cores and CPU model of the machine the CPU arm runs on."""
+    model = ""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except Exception:
+        pass
+    return {"nproc": os.cpu_count() or 1, "lscpu_model": model}
+
+
+def cpu_baseline(n, off, adj, rows, budget, procs=None, cap_s=0.0):
+    """The reference's CPU path (the oracle port of its branch-and-bound on
+    the reference's own heuristics, oracle.c) on the host cores: the sampled
+    queries go to a pool of single-threaded processes, one query at a time
+    each, under the same per-query node budget as the GPU (no wall-clock cap
+    unless cap_s > 0).  Returns a dict: the makespan of the sample, exact
+    answers (status done/heuristic) and all answers, per-query times (each
+    is the single-thread time of that query), tasks."""
     import multiprocessing as mp
-    procs = procs or min(16, os.cpu_count() or 1)
-    rows = rows[:procs]
+    procs = max(1, min(procs or (os.cpu_count() or 1), len(rows)))
     ctx = mp.get_context("spawn")
-    with ctx.Pool(len(rows), initializer=_cpu_init, initargs=(n, off, adj, cap_s)) as pool:
-        out = pool.map(_cpu_solve, [(tuple(int(x) for x in r), budget) for r in rows])
+    args = [(tuple(int(x) for x in r), budget) for r in rows]
+    with ctx.Pool(procs, initializer=_cpu_init, initargs=(n, off, adj, cap_s)) as pool:
+        pool.map(_cpu_noop, range(procs))  # processes up and the graph loaded
+        t0 = time.perf_counter()
+        out = list(pool.imap_unordered(_cpu_solve, args, chunksize=1))
+        span = time.perf_counter() - t0
     times = [o[0] for o in out]
-    capped = sum(1 for o in out if o[2] == 2)
-    qps = len(rows) / max(np.mean(times), 1e-9) if times else 0.0
-    desc = ("%d queries, one per core, node budget %d, cap %.0f s per query; "
-            "%d hit the cap, %d the node budget; mean %.2f s per query, %.0f tasks/s/core"
-            % (len(rows), budget, cap_s, capped, sum(1 for o in out if o[2] == 1),
-               float(np.mean(times)), sum(o[1] for o in out) / max(sum(times), 1e-9)))
-    return qps, len(rows), desc
+    exact = sum(1 for o in out if o[2] == 0)
+    return {"span_s": span, "queries": len(rows), "exact": exact, "procs": procs,
+            "times": times, "tasks": sum(o[1] for o in out),
+            "budget_stopped": sum(1 for o in out if o[2] == 1),
+            "capped": sum(1 for o in out if o[2] == 2)}
+
+
+def _cpu_desc(r, budget):
+    t = np.array(r["times"]) if r["times"] else np.zeros(1)
+    return ("%d queries of the step (its first ones), one per process on %d host cores, "
+            "node budget %d per query, no wall-clock cap; makespan %.1f s; %d exact, %d stopped "
+            "by the budget; single-thread %.2f s per query (mean), %.0f tasks/s per core"
+            % (r["queries"], r["procs"], budget, r["span_s"], r["exact"], r["budget_stopped"],
+               float(t.mean()), r["tasks"] / max(float(t.sum()), 1e-9)))
 
 
 _CPU_G = None
@@ -169,7 +199,14 @@ def _cpu_init(n, off, adj, cap_s):
     O.lib().orc_set_time_limit(cap_s)
 
 
+def _cpu_noop(_):
+    return 0
+
+
 def _cpu_solve(args):
+    """One query on one core.  Status as the engine reports it: 0 exact
+    (search finished, or the incumbent is optimal), 1 stopped by the node
+    budget, 2 stopped by a wall-clock cap."""
     row, budget = args
     l, h, q, hf, ld = row
     t0 = time.perf_counter()
@@ -178,6 +215,11 @@ def _cpu_solve(args):
 
 
 def run_reference(args):
+    """--impl reference: the reference's CPU path on the host cores, on the
+    same workload, metric and node budget as the GPU arm.  Each step times a
+    sample of the step's queries (its first --ref-sample) on all host cores;
+    value = exact answers / measured makespan.  Warm-up steps run a few other
+    queries (seed 43) under a small budget, only to start the processes."""
     rank, world, _ = env_rank()
     if rank != 0:
         return 0
@@ -185,25 +227,34 @@ def run_reference(args):
     import oracle as O
     og = O.OracleGraph(n, off, adj)
     rows = queries_for(og.core, args.batch * args.steps, 42)
-    warm = queries_for(og.core, args.warmup_batch * args.warmup, 43)
-    procs = min(16, os.cpu_count() or 1)
+    warm = queries_for(og.core, 8 * max(args.warmup, 1), 43)
+    procs = os.cpu_count() or 1
     for i in range(args.warmup):
-        cpu_baseline(n, off, adj, warm[i * args.warmup_batch:(i + 1) * args.warmup_batch],
-                     args.node_budget, cap_s=args.cpu_cap, procs=procs)
-    vals, samples = [], []
+        cpu_baseline(n, off, adj, warm[i * 8:(i + 1) * 8], 1000, procs=procs)
+    spans, exact, total, last = 0.0, 0, 0, None
     for i in range(args.steps):
-        qps, cores, sample = cpu_baseline(n, off, adj, rows[i * args.batch:(i + 1) * args.batch],
-                                          args.node_budget, cap_s=args.cpu_cap, procs=procs)
-        vals.append(qps)
-        samples.append(sample)
-    v = float(np.mean(vals))
+        step_rows = rows[i * args.batch:(i + 1) * args.batch][: args.ref_sample]
+        r = cpu_baseline(n, off, adj, step_rows, args.node_budget, procs=procs)
+        spans += r["span_s"]
+        exact += r["exact"]
+        total += r["queries"]
+        last = r
+    v = exact / spans if spans > 0 else 0.0
+    t = np.array(last["times"])
+    info = host_cpu_info()
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * args.batch / v,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * spans / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
-            "data": "synthetic", "config": {"workload": WORKLOAD, "batch": args.batch,
-                                            "node_budget": args.node_budget},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": procs, "kind": "port",
-                             "sample": "per step (first of %d): " % len(samples) + samples[0]},
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD, "batch": args.batch, "sample_per_step": args.ref_sample,
+                       "node_budget": args.node_budget, "wall_cap": None,
+                       "all_answers_per_s": total / spans if spans > 0 else 0.0,
+                       "exact_fraction": exact / max(total, 1),
+                       "single_thread_s_per_query": float(t.mean()),
+                       "single_thread_exact_per_s": last["exact"] / max(float(t.sum()), 1e-9),
+                       **info},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": last["procs"], "kind": "port",
+                             "sample": _cpu_desc(last, args.node_budget)},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
@@ -277,8 +328,8 @@ def main():
     ap.add_argument("--warmup-batch", type=int, default=48)
     ap.add_argument("--node-budget", type=int, default=100000)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cpu-cap", type=float, default=10.0,
-                    help="wall-clock cap per query on the CPU arms (seconds)")
+    ap.add_argument("--ref-sample", type=int, default=32,
+                    help="--impl reference: queries of each step timed on the host cores")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ctas-per-sm", type=int, default=0,
                     help="search CTAs per SM (0: autotuned on the warm-up queries)")
@@ -367,6 +418,11 @@ def main():
                                              "cuda")
     lat = np.array([r["latency_ns"] for r in results]) / 1e6
     exact = sum(1 for r in results if r["status"] in (0, 1))
+    exact_all = exact
+    if dist is not None:
+        ex = torch.tensor([float(exact)], dtype=torch.float64, device="cuda")
+        dist.all_reduce(ex)
+        exact_all = int(ex[0])
     verified = sum(1 for r in results if r["h_verified"])
     search_ns = st1["search_ns"] - st0["search_ns"]
     nbytes = st1["bytes"] - st0["bytes"]
@@ -383,12 +439,14 @@ def main():
         except Exception:
             traffic = None
     line = {
-        "metric": METRIC, "value": total_q / t_dev, "unit": UNIT, "n_gpus": world,
+        "metric": METRIC, "value": exact_all / t_dev, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * t_dev / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
         "data": "synthetic",
         "config": {"workload": WORKLOAD, "graph": "R-MAT scale 15, 524288 edges",
-                   "queries": total_q, "batch": args.batch, "node_budget": args.node_budget,
+                   "queries": total_q, "exact_answers": exact_all,
+                   "all_answers_per_s": total_q / t_dev,
+                   "batch": args.batch, "node_budget": args.node_budget,
                    "l2": "flushed between steps (256 MB write)",
                    "exact_fraction": exact / max(len(results), 1),
                    "verified_fraction": verified / max(len(results), 1),
@@ -404,7 +462,7 @@ def main():
                      "launches": slices,
                      "algorithmic_bytes_per_launch": nbytes / max(slices, 1),
                      "mean_launch_ms": search_ns / 1e6 / max(slices, 1)},
-        "e2e": {"value": total_q / wall, "unit": UNIT,
+        "e2e": {"value": exact_all / wall, "unit": UNIT, "all_answers_per_s": total_q / wall,
                 "h2d_bytes_per_step": (st1["h2d_bytes"] - st0["h2d_bytes"]) // max(args.steps, 1)
                 + 20 * args.batch,
                 "d2h_bytes_per_step": (st1["d2h_bytes"] - st0["d2h_bytes"]) // max(args.steps, 1)},
@@ -412,10 +470,13 @@ def main():
         "clocks": ck,
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        sample = rows[: min(64, len(rows))]
-        qps, cores, desc = cpu_baseline(n, off, adj, sample, args.node_budget, args.cpu_cap)
-        line["cpu_baseline"] = {"value": qps, "unit": UNIT, "cores": cores, "kind": "port",
-                                "sample": desc}
+        # one query per host core from the start of the step, same budget,
+        # no wall-clock cap (one wave: about a budget-stopped query's time)
+        procs = os.cpu_count() or 1
+        r = cpu_baseline(n, off, adj, rows[: min(procs, len(rows))], args.node_budget, procs=procs)
+        line["cpu_baseline"] = {"value": r["exact"] / r["span_s"] if r["span_s"] > 0 else 0.0,
+                                "unit": UNIT, "cores": r["procs"], "kind": "port",
+                                "sample": _cpu_desc(r, args.node_budget), **host_cpu_info()}
     eng.close()
     if rank == 0:
         print(json.dumps(line))

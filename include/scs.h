@@ -161,7 +161,9 @@ enum {
                              (larger local graphs keep them in device memory) */
   SCS_STAT_ERRORS = 15,   /* device error flags seen so far (bits, OR-ed) */
   SCS_STAT_ACTIVE = 16,   /* queries searched at once (the active target) */
-  SCS_STAT_RELEASES = 17  /* prepared queries released to the search */
+  SCS_STAT_RELEASES = 17, /* prepared queries released to the search */
+  SCS_STAT_SLIDES = 18    /* task-stack slides: a CTA's live records moved
+                             down over the room donations left below them */
 };
 int scs_stats(scs_engine *e, uint64_t *out);
 
@@ -258,11 +260,15 @@ int scs_format_result_row(const scs_result *r, char *buf, uint32_t cap);
  * q_local, padded entries used, status: 0 ok, 1 loc_adj_cap too small}.
  * Scratch is a fixed array inside the library for graphs of at most
  * SCS_NOALLOC_MAX_N vertices (about 6 MB, held on every GPU that loads the
- * library until exit); larger n is rejected with SCS_EINVAL.  The first call
- * on a device looks up the array's device address, so make it before any
- * stream capture.  All calls share the array: calls that overlap on the GPU
- * race.  The kernel is enqueued on `stream` (a cudaStream_t, NULL for the
- * default stream); results are ready when the stream is. */
+ * library until exit); larger n is rejected with SCS_EINVAL, and so is a
+ * distance bound ubd >= 65535 (hop distances are held as 16-bit values).  The
+ * first call on a device looks up the array's device address there, so make
+ * it before any stream capture; after a device reset the next call looks it
+ * up again.  An error already pending from the caller's earlier CUDA work is
+ * reported as SCS_ECUDA and left pending.  All calls share the array: calls
+ * that overlap on the GPU race.  The kernel is enqueued on `stream` (a
+ * cudaStream_t, NULL for the default stream); results are ready when the
+ * stream is. */
 #define SCS_NOALLOC_MAX_N (1u << 19)
 int scs_local_graph_noalloc(const uint32_t *d_off, const uint32_t *d_adj,
                             const uint32_t *d_core, uint32_t n, uint32_t dmax,

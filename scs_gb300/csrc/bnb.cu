@@ -1858,6 +1858,12 @@ __device__ void stack_make_room(const SearchParams &P, uint32_t *sbase,
   __syncthreads();
   if (t0 + len <= P.stk.words || b0 == 0) return;
   const unsigned long long used = t0 - b0, shift = b0;
+  // A slide copies the whole live part in chunks of at most the gap, one
+  // barrier each.  Slide only when the gap holds the record and is at least
+  // an eighth of the live part; otherwise the record goes to the pool (not
+  // sliding is always safe: reservations fall back to the pool).
+  if (shift < len || 8 * shift < used) return;
+  if (threadIdx.x == 0) atomicAdd(&P.ctr->slides, 1ull);
   for (unsigned long long base = 0; base < used; base += shift) {
     unsigned long long cnt = min(shift, used - base);
     for (unsigned long long i = threadIdx.x; i < cnt; i += BT)

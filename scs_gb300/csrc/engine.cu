@@ -465,6 +465,7 @@ static int admit(scs_engine *E) {
   }
   if (batch.empty()) return 0;
   std::vector<PrepJob> jobs;
+  std::vector<std::shared_ptr<Job>> searched;  // the jobs behind `jobs`
   size_t fs = 0;
   for (size_t i = 0; i < batch.size(); i++) {
     const Pending &p = batch[i]->p;
@@ -479,12 +480,7 @@ static int admit(scs_engine *E) {
       finish_now(E, p, a.kl, a.kl == a.ku ? SCS_HEURISTIC : SCS_DONE, a.kl, a.H);
       continue;
     }
-    uint32_t si = free_slots[fs++];
-    SlotHost &sh = E->slots[si];
-    sh.busy = true;
-    sh.p = p;
-    sh.kl_heu = a.kl;
-    sh.heuH = a.H;
+    const uint32_t si = free_slots[fs++];
     PrepJob j{};
     j.slot = si;
     j.q = p.q.q;
@@ -501,24 +497,47 @@ static int admit(scs_engine *E) {
     j.root_off_hi = (uint32_t)(roff >> 32);
     j.node_budget = E->cfg.node_budget;
     jobs.push_back(j);
+    searched.push_back(batch[i]);
+  }
+  if (jobs.empty()) return 0;
+  // The copy, the events and the launch come before any slot changes state:
+  // if one fails, the jobs go back to the head of the queue in their order
+  // and no slot is left marked busy without a preparation behind it.
+  auto requeue = [&](cudaError_t e, const char *what) {
+    {
+      std::lock_guard<std::mutex> lk(E->heu_mu);
+      for (size_t k = searched.size(); k-- > 0;) E->queue.push_front(searched[k]);
+    }
+    return E->cuda_fail(e, what);
+  };
+  cudaError_t e = cudaMemcpyAsync(E->d_jobs, jobs.data(), jobs.size() * sizeof(PrepJob),
+                                  cudaMemcpyHostToDevice, E->stream);
+  if (e != cudaSuccess) return requeue(e, "prep job copy");
+  e = cudaEventRecord(E->ev2, E->stream);
+  if (e != cudaSuccess) return requeue(e, "prep start event");
+  prep_kernel<<<(unsigned)jobs.size(), PREP_THREADS, 0, E->stream>>>(
+      DevGraph{E->g.n, E->g.dmax, E->d_off, E->d_adj, E->d_core}, E->sa, E->d_slots,
+      E->d_jobs, (int)jobs.size(), E->ps, E->pool, E->d_ctr);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return requeue(e, "prep_kernel launch");
+  E->stats[SCS_STAT_H2D] += jobs.size() * sizeof(PrepJob);
+  E->stats[SCS_STAT_LAUNCHES]++;
+  for (size_t k = 0; k < jobs.size(); k++) {
+    const uint32_t si = jobs[k].slot;
+    SlotHost &sh = E->slots[si];
+    sh.busy = true;
+    sh.p = searched[k]->p;
+    sh.kl_heu = searched[k]->kl;
+    sh.heuH = searched[k]->H;
     sh.parked = true;
     E->h_slots[si].n_local = 0;  // unknown until the next read-back
     E->parked.push_back(si);
     E->n_parked++;
   }
-  if (jobs.empty()) return 0;
-  CK(cudaMemcpyAsync(E->d_jobs, jobs.data(), jobs.size() * sizeof(PrepJob),
-                     cudaMemcpyHostToDevice, E->stream));
-  E->stats[SCS_STAT_H2D] += jobs.size() * sizeof(PrepJob);
-  CK(cudaEventRecord(E->ev2, E->stream));
-  prep_kernel<<<(unsigned)jobs.size(), PREP_THREADS, 0, E->stream>>>(
-      DevGraph{E->g.n, E->g.dmax, E->d_off, E->d_adj, E->d_core}, E->sa, E->d_slots,
-      E->d_jobs, (int)jobs.size(), E->ps, E->pool, E->d_ctr);
-  CK(cudaGetLastError());
-  CK(cudaEventRecord(E->ev3, E->stream));
-  E->prep_pending = true;
-  E->stats[SCS_STAT_LAUNCHES]++;
   E->running += (uint32_t)jobs.size();
+  // the launch is in flight: a failed end event only loses its timing
+  E->prep_pending = cudaEventRecord(E->ev3, E->stream) == cudaSuccess;
+  if (!E->prep_pending) cudaGetLastError();
   return (int)jobs.size();
 }
 
@@ -616,6 +635,7 @@ static int slice(scs_engine *E) {
   E->stats[SCS_STAT_DONATIONS] = hc.donations;
   E->stats[SCS_STAT_STEALS] = hc.steals;
   E->stats[SCS_STAT_SPILLS] = hc.spills;
+  E->stats[SCS_STAT_SLIDES] = hc.slides;
   E->stats[SCS_STAT_PREP_BYTES] = hc.prep_bytes;
   if (hc.error) {
     E->err = "device error flags " + std::to_string(hc.error) + " info " +

@@ -85,10 +85,47 @@ local_graph_noalloc_kernel(DevGraph g, uint32_t q, uint32_t kl, uint32_t ubd,
 using namespace scs;
 
 namespace {
+// Set-up state, one entry per device ordinal: the device address of the
+// scratch array and the unique id of the CUDA context it was looked up in.
+// A device reset (cudaDeviceReset) destroys that context; the next call sees
+// a new context id and does the set-up again, so a stale address is never
+// passed to the kernel.
 constexpr int MAX_DEVICES = 64;
+typedef int (*CtxGetCurrentFn)(void **);
+typedef int (*CtxGetIdFn)(void *, unsigned long long *);
 std::mutex g_mu;
+bool g_fn_ready = false;
+CtxGetCurrentFn g_ctx_current = nullptr;
+CtxGetIdFn g_ctx_id = nullptr;
 void *g_scratch_ptr[MAX_DEVICES];
-bool g_scratch_ready[MAX_DEVICES];
+unsigned long long g_scratch_ctx[MAX_DEVICES];  // 0: not set up
+
+// Id of the context current on this thread (0 if none or unavailable).  The
+// driver calls are reached through the runtime's entry-point table, so the
+// library needs no link against the driver library.
+unsigned long long current_ctx_id() {
+  if (!g_fn_ready) {
+    void *a = nullptr, *b = nullptr;
+    cudaDriverEntryPointQueryResult qa, qb;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000,
+                                         cudaEnableDefault, &qa) == cudaSuccess &&
+        qa == cudaDriverEntryPointSuccess &&
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000,
+                                         cudaEnableDefault, &qb) == cudaSuccess &&
+        qb == cudaDriverEntryPointSuccess) {
+      g_ctx_current = (CtxGetCurrentFn)a;
+      g_ctx_id = (CtxGetIdFn)b;
+    }
+    cudaGetLastError();
+    g_fn_ready = true;
+  }
+  if (!g_ctx_current || !g_ctx_id) return 0;
+  void *ctx = nullptr;
+  unsigned long long id = 0;
+  if (g_ctx_current(&ctx) != 0 || !ctx) return 0;
+  if (g_ctx_id(ctx, &id) != 0) return 0;
+  return id + 1;  // never 0
+}
 }  // namespace
 
 extern "C" {
@@ -104,20 +141,40 @@ int scs_local_graph_noalloc(const uint32_t *d_off, const uint32_t *d_adj,
       !d_loc_adj || !d_info)
     return SCS_EINVAL;
   if (n == 0 || n > NOALLOC_MAX_N || q >= n) return SCS_EINVAL;
+  // hop distances are kept as u16 with 0xFFFF meaning "not reached", so a
+  // bound at or above 0xFFFF would let unreached vertices pass the filter
+  if (ubd >= INF16) return SCS_EINVAL;
+  // an error left pending by the caller's earlier work stays pending for the
+  // caller: report it without consuming it
+  if (cudaPeekAtLastError() != cudaSuccess) return SCS_ECUDA;
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEVICES)
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEVICES) {
+    cudaGetLastError();
     return SCS_ECUDA;
+  }
   void *scratch = nullptr;
   {
-    // once per device, with that device current: the device address of the
-    // scratch array (the host-side symbol is only a stand-in)
+    // Set-up, once per device and context, with that device current: the
+    // device address of the scratch array (the host-side symbol is only a
+    // stand-in).  The first call on a device does it and loads this module
+    // there, so make that call before any stream capture.
     std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_scratch_ready[dev]) {
-      void *p = nullptr;
-      if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p)
+    unsigned long long ctx = current_ctx_id();
+    if (ctx == 0) {  // no context current yet: make the device's current
+      if (cudaSetDevice(dev) != cudaSuccess) {
+        cudaGetLastError();
         return SCS_ECUDA;
+      }
+      ctx = current_ctx_id();
+    }
+    if (ctx == 0 || g_scratch_ctx[dev] != ctx) {
+      void *p = nullptr;
+      if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) {
+        cudaGetLastError();  // the failed lookup's own error
+        return SCS_ECUDA;
+      }
       g_scratch_ptr[dev] = p;
-      g_scratch_ready[dev] = true;
+      g_scratch_ctx[dev] = ctx;  // 0 (ids unavailable): look up every call
     }
     scratch = g_scratch_ptr[dev];
   }
@@ -125,6 +182,7 @@ int scs_local_graph_noalloc(const uint32_t *d_off, const uint32_t *d_adj,
   local_graph_noalloc_kernel<<<1, PREP_THREADS, 0, (cudaStream_t)stream>>>(
       g, q, kl, ubd, (unsigned char *)scratch, d_gid, d_dist, d_loc_off,
       d_loc_adj, loc_adj_cap, d_info);
+  // no error was pending before the launch, so this one is the launch's own
   if (cudaGetLastError() != cudaSuccess) return SCS_ECUDA;
   return 0;
 }

@@ -113,6 +113,7 @@ struct Counters {
   unsigned long long phase_cycles[8];  // load, mindeg+r3, r12, bounds, ustar, doms, kids, other
   unsigned long long r12_rounds, r3_rounds, steps;
   unsigned long long sub_cycles[4], sub_counts[4];
+  unsigned long long slides;   // task-stack slides (live part moved down)
 };
 
 constexpr uint32_t ERR_SPIN = 1, ERR_POOL = 2, ERR_STACK = 4, ERR_RECORD = 8;

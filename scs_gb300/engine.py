@@ -24,7 +24,7 @@ STATUS_NAMES = {DONE: "done", HEURISTIC: "heuristic", CAPACITY: "capacity",
 STAT_NAMES = ["nodes", "slices", "donations", "steals", "spills", "bytes",
               "prep_bytes", "search_ns", "prep_ns", "launches", "h2d_bytes",
               "d2h_bytes", "heur_ns", "ctas", "smem_words", "errors", "active",
-              "releases"]
+              "releases", "slides"]
 
 
 class Config(C.Structure):

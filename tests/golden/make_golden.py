@@ -127,8 +127,8 @@ def make_brute():
 
 if __name__ == "__main__":
     what = sys.argv[1] if len(sys.argv) > 1 else "all"
-    tmp = os.path.join(ROOT, "_work", "golden_graphs")
-    os.makedirs(tmp, exist_ok=True)
+    import tempfile
+    tmp = tempfile.mkdtemp(prefix="scs_golden_")
     from oracle import build_ref
     build_ref.build_oracle()
     if what in ("heuristic", "all"):

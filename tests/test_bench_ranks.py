@@ -52,7 +52,8 @@ def test_reference_arm_prints_the_contract_line():
     import sys
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
     r = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--steps", "1",
-                        "--warmup", "0", "--batch", "4", "--cpu-cap", "1"],
+                        "--warmup", "0", "--batch", "4", "--ref-sample", "4",
+                        "--node-budget", "300"],
                        cwd=root, capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr[-2000:]
     line = json.loads(r.stdout.strip().splitlines()[-1])
@@ -60,6 +61,10 @@ def test_reference_arm_prints_the_contract_line():
     for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step",
               "higher_is_better", "cpu_baseline", "e2e", "config"):
         assert k in line, k
-    assert line["value"] > 0
+    # value counts exact answers only; the sample ran under the same budget
+    assert line["value"] >= 0 and line["config"]["all_answers_per_s"] > 0
+    assert line["ms_per_step"] > 0 and line["config"]["sample_per_step"] == 4
+    assert line["config"]["node_budget"] == 300 and line["config"]["wall_cap"] is None
+    assert line["config"]["nproc"] >= 1
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0

@@ -10,7 +10,11 @@ import pytest
 from conftest import ROOT, random_graph
 
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-REF = "/root/reference"
+
+
+def _ref_dir():
+    from oracle.build_ref import ref_dir
+    return ref_dir()
 
 
 def _golden_graph(name):
@@ -156,7 +160,7 @@ def test_engine_without_gpu_fails_loudly():
         Engine(csr=(n, off, adj), limit_queries=2)
 
 
-@pytest.mark.skipif(not os.path.isdir(REF), reason="reference tree absent")
+@pytest.mark.skipif(_ref_dir() is None, reason="reference tree absent (set SCS_REF_DIR)")
 def test_reference_sample_graphs_live(oracle_lib):
     """On the reference's own sample graphs and query files, the reference's
     compiled CPU code and the oracle agree (loader, cores, BFS, heuristics)."""
@@ -190,8 +194,8 @@ print(n)
     for graph, qf in (("data/graph.txt", "client/query/exp1_2/100"),
                       ("data/100.txt", "client/query/exp1_2/100"),
                       ("data/hepPH_SCS", "client/query/exp1_2/hepPh")):
-        out = subprocess.run([sys.executable, "-c", code, os.path.join(REF, graph),
-                              os.path.join(REF, qf)], capture_output=True, text=True)
+        out = subprocess.run([sys.executable, "-c", code, os.path.join(_ref_dir(), graph),
+                              os.path.join(_ref_dir(), qf)], capture_output=True, text=True)
         assert out.returncode == 0, out.stderr[-2000:]
 
 

@@ -1,6 +1,7 @@
 """The allocation-free local-graph entry point (scs_local_graph_noalloc),
 for callers that cannot allocate device memory, against the engine's own
-preprocessing entry point on the same queries.
+preprocessing entry point and the CPU oracle's local graph on the same
+queries, plus its argument checks.
 
 This file is named to be collected last.  It passes both alone in a fresh
 process and after the other tests: the entry point looks up its fixed scratch
@@ -25,7 +26,7 @@ def _strip(off, adj, nl):
 def test_noalloc_matches_engine_two_calls_in_a_row(oracle_lib):
     import torch
     from scs_gb300 import workloads as W
-    from scs_gb300.engine import Engine, local_graph_noalloc
+    from scs_gb300.engine import Engine, SCSError, local_graph_noalloc
     n, u, v = W.chung_lu(4000, 88000, 2.5)
     off, adj = W.to_csr(n, u, v)
     og = oracle_lib.OracleGraph(n, off, adj)
@@ -66,4 +67,18 @@ def test_noalloc_matches_engine_two_calls_in_a_row(oracle_lib):
         assert np.array_equal(so, g_off.astype(np.int64))
         assert np.array_equal(sa, g_adj)
         assert np.array_equal(dist.cpu().numpy().view(np.uint32)[:m], g_dist)
+        # and directly against the oracle's local graph
+        ctx = oracle_lib.OracleCtx(og, l, h, q, kl, ubd, 10)
+        assert m == ctx.n and int(inf[1]) == ctx.q_local
+        assert np.array_equal(gid.cpu().numpy().view(np.uint32)[:m], ctx.gid)
+        assert np.array_equal(so, ctx.off.astype(np.int64))
+        assert np.array_equal(sa, ctx.adj)
+        assert np.array_equal(dist.cpu().numpy().view(np.uint32)[:m], ctx.dist)
+        ctx.close()
+    # a distance bound the 16-bit distances cannot hold is rejected
+    l, h, q, ubd, kl = cases[0]
+    with pytest.raises(SCSError, match=r"\(-1\)"):
+        local_graph_noalloc(d_off.data_ptr(), d_adj.data_ptr(), d_core.data_ptr(), n,
+                            og.dmax, q, kl, 0xFFFF, gid.data_ptr(), dist.data_ptr(),
+                            loff.data_ptr(), ladj.data_ptr(), cap, info.data_ptr(), stream)
     eng.close()
