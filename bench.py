@@ -367,17 +367,19 @@ def main():
     from scs_gb300.engine import core_numbers
     core = core_numbers(n, off, adj)
     warm = queries_for(core, args.warmup_batch * args.warmup, 43 + 1000 * rank)
-    tune = {"ctas_per_sm": args.ctas_per_sm, "slice_us": args.slice_us or 80000}
+    tune = {"ctas_per_sm": args.ctas_per_sm, "slice_us": args.slice_us or 80000,
+            "active_queries": args.active_queries, "stack_words": args.stack_words}
+    trials = None
     if not args.ctas_per_sm:
         # launch shape chosen by the autotuner on warm-up queries (not timed)
         from scs_gb300.autotune import autotune
         sample = [tuple(int(x) for x in r) for r in warm[: min(len(warm), 64)]]
-        tune, _ = autotune(n, off, adj, sample, args.node_budget, device=local)
+        tune, trials = autotune(n, off, adj, sample, args.node_budget, device=local)
     eng = Engine(csr=(n, off, adj), limit_queries=max(args.batch, 1),
                  slice_us=tune["slice_us"], ctas_per_sm=tune["ctas_per_sm"],
-                 node_budget=args.node_budget, stack_words=args.stack_words,
+                 node_budget=args.node_budget, stack_words=tune["stack_words"],
                  pool_words=args.pool_words, device=local,
-                 active_queries=args.active_queries, release_order=args.release_order)
+                 active_queries=tune["active_queries"], release_order=args.release_order)
     # weak scaling: every rank runs the full 1,000-query workload of its own
     # query seed (rank 0 uses the workload's seed 42)
     rows = queries_for(core, args.batch * args.steps, 42 + 1000 * rank)
@@ -455,7 +457,8 @@ def main():
                    "ctas_per_sm": tune["ctas_per_sm"],
                    "resident_ctas": st1["ctas"], "smem_state_words": st1["smem_words"],
                    "active_queries": st1["active"],
-                   "slice_us": tune["slice_us"]},
+                   "slice_us": tune["slice_us"], "stack_words": tune["stack_words"],
+                   "autotune_trials": trials},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak if peak else None, "traffic": traffic,
                      "peak_kind": peak_kind, "kernel": "search_kernel",

@@ -162,8 +162,10 @@ enum {
   SCS_STAT_ERRORS = 15,   /* device error flags seen so far (bits, OR-ed) */
   SCS_STAT_ACTIVE = 16,   /* queries searched at once (the active target) */
   SCS_STAT_RELEASES = 17, /* prepared queries released to the search */
-  SCS_STAT_SLIDES = 18    /* task-stack slides: a CTA's live records moved
+  SCS_STAT_SLIDES = 18,   /* task-stack slides: a CTA's live records moved
                              down over the room donations left below them */
+  SCS_STAT_PROPOSALS_BETTER = 19 /* learned incumbent proposals that raised
+                             a query's incumbent (model loaded) */
 };
 int scs_stats(scs_engine *e, uint64_t *out);
 
@@ -277,6 +279,66 @@ int scs_local_graph_noalloc(const uint32_t *d_off, const uint32_t *d_adj,
                             uint32_t *d_loc_off, uint32_t *d_loc_adj,
                             uint64_t loc_adj_cap, uint32_t *d_info,
                             void *stream);
+
+/* ---- learned branching (no counterpart in the reference) ----
+ * A small network (16 candidate features -> 128 -> 128 -> 1, ReLU) scores
+ * the branching candidates of each search step: the engine takes u* from a
+ * shortlist of the candidates the reference's rule accepts (selectUstar,
+ * src/helpers.cc:1104-1168), by the largest network score instead of the
+ * rule's score.  Every pruning rule and the optimality proof stay the
+ * integer method, so answers are the same with or without a model.  The
+ * network runs on the tensor cores in BF16 with FP32 accumulation; its FP32
+ * weights are trained by the engine's own GPU kernels (scs_mlp_train) on
+ * traces the exact solver emits (scs_trace_enable / scs_trace_read). */
+
+/* Load a model file ("SCSMLP01", u32 dims {16,128,128,1}, then the FP32
+ * parameters W1[16][128], b1[128], W2[128][128], b2[128], W3[128], b3);
+ * NULL returns the engine to the plain method.  Needs an idle engine. */
+int scs_load_model(scs_engine *e, const char *path);
+
+/* Record the shortlisted candidates of sampled search steps: per record 16
+ * FP32 features and the key {query tag (low 32 bits of the ticket), global
+ * vertex id}.  A CTA records its steps whose step count has the low
+ * sample_shift bits zero.  max_records = 0 turns the trace off.  Needs an
+ * idle engine; resets the record count. */
+int scs_trace_enable(scs_engine *e, uint64_t max_records, uint32_t sample_shift);
+
+/* Copy up to max records (feat: max*16 floats, keys: max*2 words; either may
+ * be NULL); *written gets the records the search produced, which can exceed
+ * the capacity (the excess was dropped).  Returns the count copied. */
+int scs_trace_read(scs_engine *e, float *feat, uint32_t *keys, uint64_t max,
+                   uint64_t *written);
+
+#define SCS_MLP_NPARAM 18817
+typedef struct {
+  uint32_t epochs;     /* passes over the samples (0: 20) */
+  uint32_t batch;      /* samples per step (0: 4096) */
+  float lr;            /* Adam step size (0: 1e-3) */
+  float weight_decay;  /* L2 term added to the gradient */
+  uint64_t seed;       /* shuffling */
+} scs_mlp_train_cfg;
+
+/* Train on the GPU (hand-written FP32 kernels, Adam, weighted binary
+ * cross-entropy on the logit) from X[n][16], labels y[n] in {0,1} and
+ * weights w[n] (NULL: all 1).  params (SCS_MLP_NPARAM floats, file order)
+ * holds the initial values and receives the result; epoch_loss (may be
+ * NULL) gets the mean loss of each epoch. */
+int scs_mlp_train(const float *X, const float *y, const float *w, uint64_t n,
+                  const scs_mlp_train_cfg *cfg, float *params, float *epoch_loss,
+                  int device);
+
+/* Weighted mean loss and its gradient (file order) on one batch, computed by
+ * the training kernels (for checking them against a CPU restatement). */
+int scs_mlp_grad(const float *params, const float *X, const float *y, const float *w,
+                 uint64_t n, double *loss, float *grad, int device);
+
+/* Logits of n feature rows by the tensor-core BF16 inference the search
+ * kernel uses (one warp per 16 rows). */
+int scs_mlp_infer(const float *params, const float *X, uint64_t n, float *out,
+                  int device);
+
+/* Text of the last error of the scs_mlp_* calls. */
+const char *scs_mlp_last_error(void);
 
 /* ---- test hooks (used by the parity tests; no reference counterpart) ----
  * These expose single stages of the pipeline so they can be compared with

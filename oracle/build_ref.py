@@ -25,7 +25,7 @@ DEFAULT_REF = "/root/reference"
 
 def ref_dir():
     """The reference tree to build from, or None when it is not present."""
-    d = os.environ.get("SCS_REF_DIR", DEFAULT_REF)
+    d = os.path.abspath(os.environ.get("SCS_REF_DIR", DEFAULT_REF))
     return d if os.path.isdir(d) else None
 
 
@@ -70,7 +70,7 @@ def build_ref(src=None, verbose=False):
 def build_ref_server(src=None, verbose=False):
     """Compile the reference's main.cu unchanged into oracle/_ref; returns
     the executable's path or None when the tree or nvcc is absent."""
-    src = src or ref_dir()
+    src = os.path.abspath(src) if src else ref_dir()
     if not src or not os.path.exists(os.path.join(src, "main.cu")):
         return None
     nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"

@@ -12,7 +12,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU = ["prep.cu", "bnb.cu", "engine.cu", "noalloc.cu", "core.cu"]
+CU = ["prep.cu", "bnb.cu", "engine.cu", "noalloc.cu", "core.cu", "mlp.cu", "propose.cu"]
 CXX = ["host_graph.cpp", "host_api.cpp"]
 LIB = "libscs.so"
 EXES = {"scs_server": "server.cpp", "scs_client": "client.cpp", "scs_verify": "verify.cpp"}

@@ -20,6 +20,7 @@
 // dive), the others go to the CTA's own LIFO stack in HBM, and the oldest
 // stack entry is donated to a shared pool when other CTAs are idle.  Every
 // spin-wait has an iteration bound and reports through Counters::error.
+#include "mlp.cuh"
 #include "scs_device.cuh"
 
 namespace scs {
@@ -126,6 +127,15 @@ struct Sh {
   uint32_t kid_len[MAX_DOMS + 2];
   unsigned long long kid_dst[MAX_DOMS + 2];
   unsigned long long kid_pool[MAX_DOMS + 2];
+  // learned branching (mlp.cuh): lrn bit 0 = the network picks u* among the
+  // shortlist, bit 1 = this step's shortlist goes to the trace
+  uint32_t lrn;
+  uint32_t nsl;      // shortlisted candidates (<= 16)
+  uint32_t nstep;    // steps this CTA ran (trace sampling)
+  uint32_t qtag;     // the query's tag (trace key)
+  uint32_t sl_id[MLP_TILE], sl_pos[MLP_TILE];
+  double sl_sc[MLP_TILE];
+  float feat[MLP_TILE * (MLP_IN + 1)];
 };
 
 __device__ __forceinline__ uint32_t st_of(uint32_t w) { return w >> 30; }
@@ -1084,7 +1094,141 @@ __device__ bool score_candidates(Task &T, Sh &sh) {
   return false;
 }
 
-__device__ void choose_ustar(Task &T, Sh &sh) {
+// Shortlist for the network: the two best per-thread candidates of each warp
+// (by the reference rule's score, ties to the smaller id), so the rule's own
+// u* is always in it.  All threads call; slots without a candidate get
+// UINT32_MAX.  sc/id/pos are each thread's best candidate.
+static_assert(2 * NWARP == MLP_TILE, "two shortlist places per warp");
+__device__ void shortlist(double sc, uint32_t id, uint32_t pos, Sh &sh) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < 2; k++) {
+    double s = sc;
+    uint32_t i = id;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+      const double s2 = __shfl_xor_sync(0xffffffffu, s, o);
+      const uint32_t i2 = __shfl_xor_sync(0xffffffffu, i, o);
+      if (s2 > s || (s2 == s && i2 < i)) {
+        s = s2;
+        i = i2;
+      }
+    }
+    const bool ok = i != UINT32_MAX && s > 0.0;
+    const bool mine = ok && id == i;
+    const unsigned m = __ballot_sync(0xffffffffu, mine);
+    const uint32_t p = __shfl_sync(0xffffffffu, pos, m ? __ffs(m) - 1 : 0);
+    if (lane == 0) {
+      sh.sl_sc[2 * wid + k] = ok ? s : 0.0;
+      sh.sl_id[2 * wid + k] = ok ? i : UINT32_MAX;
+      sh.sl_pos[2 * wid + k] = p;
+    }
+    if (mine) {  // the next round looks for the warp's second best
+      sc = 0.0;
+      id = UINT32_MAX;
+    }
+  }
+}
+
+// The network's choice of u* among the shortlist (lrn bit 0), and the
+// shortlist's trace records (bit 1).  Warp 0 works; all threads call.
+// Features follow make_features (mlp.cuh); the choice is the largest
+// logit, ties to the smaller local id.  Any shortlisted vertex is an R
+// vertex with a C neighbour, which the branching rule accepts as u*.
+__device__ void learned_choice(const SearchParams &P, Task &T, Sh &sh) {
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    // compact the shortlist (16 places, empty ones UINT32_MAX)
+    const uint32_t id = lane < MLP_TILE ? sh.sl_id[lane] : UINT32_MAX;
+    const uint32_t pos = lane < MLP_TILE ? sh.sl_pos[lane] : 0;
+    const double sc = lane < MLP_TILE ? sh.sl_sc[lane] : 0.0;
+    const unsigned m = __ballot_sync(0xffffffffu, id != UINT32_MAX);
+    const uint32_t nsl = __popc(m);
+    const uint32_t r = __popc(m & ((1u << lane) - 1u));
+    __syncwarp();
+    if (id != UINT32_MAX) {
+      sh.sl_id[r] = id;
+      sh.sl_pos[r] = pos;
+      sh.sl_sc[r] = sc;
+    }
+    __syncwarp();
+    const bool score = (sh.lrn & 1u) && nsl >= 2;
+    const bool trace = (sh.lrn & 2u) && nsl >= 1;
+    if (score || trace) {
+      FeatTask k;
+      k.s = sh.csize + sh.nR;
+      k.csize = sh.csize;
+      k.n_local = sh.n_local;
+      k.l = sh.l;
+      k.h = sh.h;
+      k.kl = sh.kl;
+      k.ub = min(sh.p1, sh.p2);
+      k.ubd = ubd_dev(sh.kl, sh.h);
+      k.dmax = sh.dmax;
+      // the rule's best score (its u* is the first place of some warp)
+      double smax = 0.0;
+      for (uint32_t j = 0; j < nsl; j++) smax = fmax(smax, sh.sl_sc[j]);
+      if (lane < MLP_TILE) {
+        float *f = sh.feat + lane * (MLP_IN + 1);
+        if ((uint32_t)lane < nsl) {
+          const uint32_t v = sh.sl_id[lane];
+          const uint32_t w = T.W[v];
+          FeatIn c;
+          c.dC = dc_of(w);
+          c.dR = dr_of(w);
+          c.dist = T.dist[v];
+          c.core = __ldg(P.g.core + T.gid[v]);
+          c.deg = T.off[v + 1] - T.off[v];
+          c.score = (float)sh.sl_sc[lane];
+          c.score_max = (float)smax;
+          c.is_best = v == sh.ustar;
+          make_features(c, k, f);
+        } else {
+#pragma unroll
+          for (int j = 0; j < MLP_IN; j++) f[j] = 0.f;
+        }
+      }
+      __syncwarp();
+      if (score) {
+        const float z = mlp_score16(P.mlp, sh.feat, MLP_IN + 1);
+        float bz = (uint32_t)lane < nsl ? z : -INFINITY;
+        uint32_t bi = (uint32_t)lane < nsl ? sh.sl_id[lane] : UINT32_MAX;
+        uint32_t bp = (uint32_t)lane < nsl ? sh.sl_pos[lane] : 0;
+#pragma unroll
+        for (int o = 16; o; o >>= 1) {
+          const float z2 = __shfl_xor_sync(0xffffffffu, bz, o);
+          const uint32_t i2 = __shfl_xor_sync(0xffffffffu, bi, o);
+          const uint32_t p2 = __shfl_xor_sync(0xffffffffu, bp, o);
+          if (z2 > bz || (z2 == bz && i2 < bi)) {
+            bz = z2;
+            bi = i2;
+            bp = p2;
+          }
+        }
+        if (lane == 0) {
+          sh.ustar = bi;
+          sh.us_idx = bp;
+        }
+      }
+      if (trace) {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(P.trace_count, (unsigned long long)nsl);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if ((uint32_t)lane < nsl && base + lane < P.trace_cap) {
+          const float *f = sh.feat + lane * (MLP_IN + 1);
+          float *dst = P.trace_feat + (base + lane) * MLP_IN;
+#pragma unroll
+          for (int j = 0; j < MLP_IN; j++) dst[j] = f[j];
+          P.trace_key[2 * (base + lane)] = sh.qtag;
+          P.trace_key[2 * (base + lane) + 1] = T.gid[sh.sl_id[lane]];
+        }
+      }
+    }
+  }
+  __syncthreads();
+}
+
+__device__ void choose_ustar(const SearchParams &P, Task &T, Sh &sh) {
   const int t = threadIdx.x;
   const uint32_t s = sh.s;
   unsigned long long c0 = SCS_PROF_MODE == 3 ? clock64() : 0;
@@ -1168,6 +1312,7 @@ __device__ void choose_ustar(Task &T, Sh &sh) {
       }
     }
   }
+  if (sh.lrn) shortlist(best, bid, bpos, sh);  // read after block_argmax's barriers
   double osc;
   uint32_t oid;
   block_argmax(best, bid, sh, osc, oid);
@@ -1179,6 +1324,7 @@ __device__ void choose_ustar(Task &T, Sh &sh) {
     if (SCS_PROF_MODE == 3) sh.sub[2] += clock64() - c0;
   }
   __syncthreads();
+  if (sh.lrn && sh.ustar != UINT32_MAX) learned_choice(P, T, sh);
 }
 
 // reset the pushed scores (candidates are exactly the R vertices with C
@@ -1551,9 +1697,11 @@ __device__ void clear_aux_list(Task &T, Sh &sh) {
 // one step on the loaded task (phases up to the choice of u* and doms)
 // returns outcome in sh.outcome
 // ---------------------------------------------------------------------------
-__device__ void step_core(Task &T, Sh &sh, bool test, uint32_t *t_wit) {
+__device__ void step_core(const SearchParams &P, Task &T, Sh &sh, bool test,
+                          uint32_t *t_wit) {
   const int t = threadIdx.x;
   if (t == 0) {
+    sh.nstep++;
     sh.best = UINT32_MAX;
     sh.outcome = 0;
     sh.p1 = sh.p2 = UINT32_MAX;
@@ -1600,7 +1748,7 @@ __device__ void step_core(Task &T, Sh &sh, bool test, uint32_t *t_wit) {
     __syncthreads();
     return;
   }
-  choose_ustar(T, sh);
+  choose_ustar(P, T, sh);
   phase_mark(sh, 4);
   if (sh.ustar == UINT32_MAX) {
     clear_scores(T, sh);
@@ -1663,7 +1811,11 @@ __device__ void set_task_header(const SearchParams &P, Sh &sh,
     sh.kl = *(volatile uint32_t *)&sl->kl;
     sh.wit_pending = *(volatile uint32_t *)&sl->abort;
     sh.q_local = sl->q_local;
+    sh.qtag = sl->qtag;
     sh.dmax = P.g.dmax;
+    // the step after this one's increment decides the trace sampling
+    sh.lrn = (P.mlp.w ? 1u : 0u) |
+             ((P.trace_cap && ((sh.nstep + 1) & P.trace_mask) == 0) ? 2u : 0u);
     sh.mean_deg = sl->n_local ? (float)P.sa.loc_off[(size_t)sh.slot * (P.sa.stride_n + 1) + sl->n_local] /
                                     (float)sl->n_local
                               : 0.0f;
@@ -1686,6 +1838,7 @@ step_test_kernel(SearchParams P) {
   if (threadIdx.x == 0) {
     sh.kl = P.t_kl[ti];
     sh.bytes = 0;
+    sh.nstep = blockIdx.x;
     for (int i = 0; i < 8; i++) sh.ph[i] = 0;
     for (int i = 0; i < 4; i++) sh.sub[i] = sh.cnt4[i] = 0;
     sh.r12 = sh.r3 = 0;
@@ -1698,7 +1851,7 @@ step_test_kernel(SearchParams P) {
   __syncthreads();
   load_record(rec, T, sh);
   uint32_t *wit = P.t_wit + (size_t)ti * P.t_wit_stride;
-  step_core(T, sh, true, wit);
+  step_core(P, T, sh, true, wit);
   uint32_t *hdr = P.t_hdr + 16 * ti;
   uint32_t *kids = P.t_kids + (size_t)ti * P.t_kids_stride;
   if (sh.outcome == 0) {
@@ -1917,6 +2070,7 @@ search_kernel(SearchParams P) {
     sh.have = 0;
     sh.stop = 0;
     sh.bytes = 0;
+    sh.nstep = blockIdx.x;
     for (int i = 0; i < 8; i++) sh.ph[i] = 0;
     for (int i = 0; i < 4; i++) sh.sub[i] = sh.cnt4[i] = 0;
     sh.r12 = sh.r3 = 0;
@@ -2051,7 +2205,7 @@ search_kernel(SearchParams P) {
     const uint32_t s_in = sh.s;
     const unsigned long long c_step = clock64();
 #endif
-    step_core(T, sh, false, nullptr);
+    step_core(P, T, sh, false, nullptr);
 #if SCS_PROF_MODE == 2
     if (t == 0) {
       const int b = s_in < 512 ? 0 : s_in < 4096 ? 1 : 2;

@@ -14,6 +14,7 @@
 // launch per slice, and the engine returns the community itself.
 #include <algorithm>
 #include <atomic>
+#include <cmath>
 #include <chrono>
 #include <condition_variable>
 #include <memory>
@@ -134,6 +135,16 @@ struct scs_engine {
   std::vector<HeuWork> work;
   unsigned host_threads = 1;
   std::vector<void *> allocs;
+  // learned branching: packed network (learned == false: the plain method)
+  bool learned = false;
+  uint2 *d_mlp_w = nullptr;
+  float *d_mlp_b = nullptr;
+  // trace of the shortlisted candidates for training (cap 0: off)
+  float *d_trace_feat = nullptr;
+  uint32_t *d_trace_key = nullptr;
+  unsigned long long *d_trace_count = nullptr;
+  uint64_t trace_cap = 0;
+  uint32_t trace_mask = 0;
 
   int cuda_fail(cudaError_t e, const char *what) {
     err = std::string(what) + ": " + cudaGetErrorString(e);
@@ -374,6 +385,12 @@ static SearchParams make_params(scs_engine *E) {
   P.scr = E->scr;
   P.nw_smem = E->nw_smem;
   P.nslots = E->nslots;
+  P.mlp = E->learned ? MlpDev{E->d_mlp_w, E->d_mlp_b} : MlpDev{nullptr, nullptr};
+  P.trace_feat = E->d_trace_feat;
+  P.trace_key = E->d_trace_key;
+  P.trace_count = E->d_trace_count;
+  P.trace_cap = E->trace_cap;
+  P.trace_mask = E->trace_mask;
   return P;
 }
 
@@ -496,6 +513,7 @@ static int admit(scs_engine *E) {
     j.root_off_lo = (uint32_t)roff;
     j.root_off_hi = (uint32_t)(roff >> 32);
     j.node_budget = E->cfg.node_budget;
+    j.qtag = (uint32_t)p.ticket;
     jobs.push_back(j);
     searched.push_back(batch[i]);
   }
@@ -520,6 +538,15 @@ static int admit(scs_engine *E) {
       E->d_jobs, (int)jobs.size(), E->ps, E->pool, E->d_ctr);
   e = cudaGetLastError();
   if (e != cudaSuccess) return requeue(e, "prep_kernel launch");
+  if (E->learned) {
+    // the network's incumbent proposal on each new local graph (propose.cu)
+    propose_kernel<<<(unsigned)std::min<size_t>(jobs.size(), E->grid), 256, 0, E->stream>>>(
+        DevGraph{E->g.n, E->g.dmax, E->d_off, E->d_adj, E->d_core}, E->sa, E->d_slots,
+        E->d_jobs, (int)jobs.size(), E->scr, MlpDev{E->d_mlp_w, E->d_mlp_b}, E->d_ctr);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return requeue(e, "propose_kernel launch");
+    E->stats[SCS_STAT_LAUNCHES]++;
+  }
   E->stats[SCS_STAT_H2D] += jobs.size() * sizeof(PrepJob);
   E->stats[SCS_STAT_LAUNCHES]++;
   for (size_t k = 0; k < jobs.size(); k++) {
@@ -636,6 +663,7 @@ static int slice(scs_engine *E) {
   E->stats[SCS_STAT_STEALS] = hc.steals;
   E->stats[SCS_STAT_SPILLS] = hc.spills;
   E->stats[SCS_STAT_SLIDES] = hc.slides;
+  E->stats[SCS_STAT_PROPOSALS_BETTER] = hc.proposals_better;
   E->stats[SCS_STAT_PREP_BYTES] = hc.prep_bytes;
   if (hc.error) {
     E->err = "device error flags " + std::to_string(hc.error) + " info " +
@@ -837,6 +865,11 @@ int scs_destroy(scs_engine *E) {
   for (auto &t : E->heu_workers) t.join();
   if (E->stream) cudaStreamSynchronize(E->stream);
   for (void *p : E->allocs) cudaFree(p);
+  cudaFree(E->d_mlp_w);
+  cudaFree(E->d_mlp_b);
+  cudaFree(E->d_trace_feat);
+  cudaFree(E->d_trace_key);
+  cudaFree(E->d_trace_count);
   if (E->ev0) cudaEventDestroy(E->ev0);
   if (E->ev1) cudaEventDestroy(E->ev1);
   if (E->ev2) cudaEventDestroy(E->ev2);
@@ -844,6 +877,93 @@ int scs_destroy(scs_engine *E) {
   if (E->stream) cudaStreamDestroy(E->stream);
   delete E;
   return 0;
+}
+
+// ---- learned branching ----
+
+int scs_load_model(scs_engine *E, const char *path) {
+  if (!E) return SCS_EINVAL;
+  if (E->running) {
+    E->err = "scs_load_model needs an idle engine";
+    return SCS_EBUSY;
+  }
+  if (!path) {  // back to the plain method
+    E->learned = false;
+    return 0;
+  }
+  FILE *f = fopen(path, "rb");
+  if (!f) {
+    E->err = std::string("cannot open model file ") + path;
+    return SCS_EIO;
+  }
+  char magic[8] = {0};
+  uint32_t dims[4] = {0, 0, 0, 0};
+  std::vector<float> params(MLP_NPARAM);
+  const bool ok = fread(magic, 1, 8, f) == 8 && memcmp(magic, "SCSMLP01", 8) == 0 &&
+                  fread(dims, 4, 4, f) == 4 && dims[0] == (uint32_t)MLP_IN &&
+                  dims[1] == (uint32_t)MLP_H && dims[2] == (uint32_t)MLP_H && dims[3] == 1 &&
+                  fread(params.data(), 4, MLP_NPARAM, f) == (size_t)MLP_NPARAM;
+  fclose(f);
+  if (!ok) {
+    E->err = std::string("not a 16-128-128-1 model file: ") + path;
+    return SCS_EIO;
+  }
+  for (float x : params)
+    if (!std::isfinite(x)) {
+      E->err = "model file holds a non-finite parameter";
+      return SCS_EINVAL;
+    }
+  std::vector<uint32_t> packed;
+  std::vector<float> bias;
+  mlp_pack(params.data(), packed, bias);
+  CK(cudaSetDevice(E->dev));
+  if (!E->d_mlp_w) CK(cudaMalloc((void **)&E->d_mlp_w, packed.size() * 4));
+  if (!E->d_mlp_b) CK(cudaMalloc((void **)&E->d_mlp_b, bias.size() * 4));
+  CK(cudaMemcpyAsync(E->d_mlp_w, packed.data(), packed.size() * 4, cudaMemcpyHostToDevice,
+                     E->stream));
+  CK(cudaMemcpyAsync(E->d_mlp_b, bias.data(), bias.size() * 4, cudaMemcpyHostToDevice,
+                     E->stream));
+  CK(cudaStreamSynchronize(E->stream));
+  E->stats[SCS_STAT_H2D] += packed.size() * 4 + bias.size() * 4;
+  E->learned = true;
+  return 0;
+}
+
+int scs_trace_enable(scs_engine *E, uint64_t max_records, uint32_t sample_shift) {
+  if (!E || sample_shift > 20) return SCS_EINVAL;
+  if (E->running) return SCS_EBUSY;
+  CK(cudaSetDevice(E->dev));
+  CK(cudaStreamSynchronize(E->stream));
+  cudaFree(E->d_trace_feat);
+  cudaFree(E->d_trace_key);
+  E->d_trace_feat = nullptr;
+  E->d_trace_key = nullptr;
+  E->trace_cap = 0;
+  if (!max_records) return 0;
+  CK(cudaMalloc((void **)&E->d_trace_feat, max_records * MLP_IN * 4ull));
+  CK(cudaMalloc((void **)&E->d_trace_key, max_records * 8ull));
+  if (!E->d_trace_count) CK(cudaMalloc((void **)&E->d_trace_count, 8));
+  CK(cudaMemsetAsync(E->d_trace_count, 0, 8, E->stream));
+  CK(cudaStreamSynchronize(E->stream));
+  E->trace_cap = max_records;
+  E->trace_mask = (1u << sample_shift) - 1u;
+  return 0;
+}
+
+int scs_trace_read(scs_engine *E, float *feat, uint32_t *keys, uint64_t max,
+                   uint64_t *written) {
+  if (!E || !written) return SCS_EINVAL;
+  *written = 0;
+  if (!E->trace_cap) return 0;
+  unsigned long long cnt = 0;
+  CK(cudaMemcpyAsync(&cnt, E->d_trace_count, 8, cudaMemcpyDeviceToHost, E->stream));
+  CK(cudaStreamSynchronize(E->stream));
+  *written = cnt;
+  const uint64_t n = std::min<uint64_t>(std::min<uint64_t>(cnt, E->trace_cap), max);
+  if (n && feat)
+    CK(cudaMemcpy(feat, E->d_trace_feat, n * MLP_IN * 4ull, cudaMemcpyDeviceToHost));
+  if (n && keys) CK(cudaMemcpy(keys, E->d_trace_key, n * 8ull, cudaMemcpyDeviceToHost));
+  return (int)std::min<uint64_t>(n, (uint64_t)INT32_MAX);
 }
 
 }  // extern "C"

@@ -118,6 +118,7 @@ prep_kernel(DevGraph g, SlotArrays sa, Slot *slots, const PrepJob *jobs,
     sl->wit_val = 0;
     sl->wit_n = 0;
     sl->q_global = job.q;
+    sl->qtag = job.qtag;
     sl->abort = 0;
     sl->pending = 1;
     sl->nodes = 0;

@@ -21,6 +21,8 @@
 
 #include <cuda_runtime.h>
 
+#include "mlp.cuh"
+
 namespace scs {
 
 constexpr uint32_t SENT = 0xFFFFFFFFu;
@@ -58,6 +60,7 @@ struct Slot {
   uint32_t wit_val;  // min degree of the witness (0 = none)
   uint32_t wit_n;
   uint32_t q_global;
+  uint32_t qtag;     // the host's tag of the query (trace records carry it)
   uint32_t abort;    // set when the query stops early (budget/capacity)
   unsigned long long pending;  // outstanding tasks of this query
   unsigned long long nodes;
@@ -114,6 +117,8 @@ struct Counters {
   unsigned long long r12_rounds, r3_rounds, steps;
   unsigned long long sub_cycles[4], sub_counts[4];
   unsigned long long slides;   // task-stack slides (live part moved down)
+  unsigned long long proposals;         // learned incumbent proposals made
+  unsigned long long proposals_better;  // ... that raised the incumbent
 };
 
 constexpr uint32_t ERR_SPIN = 1, ERR_POOL = 2, ERR_STACK = 4, ERR_RECORD = 8;
@@ -157,6 +162,8 @@ struct PrepJob {
   uint32_t root_to_pool;  // 0: no root; 1: root published now; 2: root parked
   uint32_t root_off_lo, root_off_hi;  // parked root's arena offset (words)
   unsigned long long node_budget;
+  uint32_t qtag;
+  uint32_t pad_;
 };
 
 struct PrepScratch {
@@ -193,6 +200,15 @@ struct SearchParams {
   uint32_t *t_wit;
   uint32_t t_wit_stride;
   const uint32_t *t_kl;             // incumbent per test task
+  // learned branching: packed network (w == null: the plain method) and the
+  // trace the exact solver emits for training (cap == 0: none)
+  MlpDev mlp;
+  float *trace_feat;                // [cap][16] features
+  uint32_t *trace_key;              // [cap][2] query tag, global vertex id
+  unsigned long long *trace_count;  // records written (may pass cap)
+  unsigned long long trace_cap;
+  uint32_t trace_mask;              // a CTA traces its steps with
+                                    // (step & mask) == 0
 };
 
 constexpr int PREP_THREADS = 512;
@@ -219,5 +235,8 @@ int gpu_core_numbers(const uint32_t *d_off, const uint32_t *d_adj, uint32_t n,
                      uint32_t *d_core, uint32_t *d_scratch, void *ctr_dev,
                      void *ctr_host, int num_sms, cudaStream_t st);
 __global__ void step_test_kernel(SearchParams P);
+// learned incumbent proposal, one CTA of 256 threads per prepared job
+__global__ void propose_kernel(DevGraph g, SlotArrays sa, Slot *slots, const PrepJob *jobs,
+                               int njobs, Scratch scr, MlpDev M, Counters *ctr);
 
 }  // namespace scs

@@ -24,7 +24,7 @@ STATUS_NAMES = {DONE: "done", HEURISTIC: "heuristic", CAPACITY: "capacity",
 STAT_NAMES = ["nodes", "slices", "donations", "steals", "spills", "bytes",
               "prep_bytes", "search_ns", "prep_ns", "launches", "h2d_bytes",
               "d2h_bytes", "heur_ns", "ctas", "smem_words", "errors", "active",
-              "releases", "slides"]
+              "releases", "slides", "proposals_better"]
 
 
 class Config(C.Structure):
@@ -55,6 +55,81 @@ class Result(C.Structure):
 
 class SCSError(RuntimeError):
     pass
+
+
+class MlpTrainCfg(C.Structure):
+    _fields_ = [("epochs", C.c_uint32), ("batch", C.c_uint32), ("lr", C.c_float),
+                ("weight_decay", C.c_float), ("seed", C.c_uint64)]
+
+
+MLP_NPARAM = 18817
+MLP_IN = 16
+
+
+def _fp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def _mlp_check(rc, what):
+    if rc < 0:
+        raise SCSError("%s failed (%d): %s" % (what, rc, lib().scs_mlp_last_error().decode()))
+    return rc
+
+
+def mlp_train(X, y, params, w=None, epochs=20, batch=4096, lr=1e-3, weight_decay=0.0,
+              seed=0, device=0):
+    """Train on the GPU with the engine's own kernels; returns (params,
+    per-epoch mean loss)."""
+    X = np.ascontiguousarray(X, dtype=np.float32)
+    y = np.ascontiguousarray(y, dtype=np.float32)
+    p = np.ascontiguousarray(params, dtype=np.float32).copy()
+    assert X.shape[1] == MLP_IN and p.size == MLP_NPARAM
+    wa = None if w is None else np.ascontiguousarray(w, dtype=np.float32)
+    cfg = MlpTrainCfg(epochs, batch, lr, weight_decay, seed)
+    losses = np.zeros(epochs, dtype=np.float32)
+    _mlp_check(lib().scs_mlp_train(_fp(X), _fp(y), None if wa is None else _fp(wa), len(y),
+                                   C.byref(cfg), _fp(p), _fp(losses), device), "scs_mlp_train")
+    return p, losses
+
+
+def mlp_grad(params, X, y, w=None, device=0):
+    """(loss, gradient) of one batch computed by the GPU training kernels."""
+    X = np.ascontiguousarray(X, dtype=np.float32)
+    y = np.ascontiguousarray(y, dtype=np.float32)
+    p = np.ascontiguousarray(params, dtype=np.float32)
+    wa = None if w is None else np.ascontiguousarray(w, dtype=np.float32)
+    g = np.zeros(MLP_NPARAM, dtype=np.float32)
+    loss = C.c_double()
+    _mlp_check(lib().scs_mlp_grad(_fp(p), _fp(X), _fp(y), None if wa is None else _fp(wa),
+                                  len(y), C.byref(loss), _fp(g), device), "scs_mlp_grad")
+    return loss.value, g
+
+
+def mlp_infer(params, X, device=0):
+    """Logits of the rows of X by the tensor-core BF16 inference path."""
+    X = np.ascontiguousarray(X, dtype=np.float32)
+    p = np.ascontiguousarray(params, dtype=np.float32)
+    out = np.zeros(len(X), dtype=np.float32)
+    _mlp_check(lib().scs_mlp_infer(_fp(p), _fp(X), len(X), _fp(out), device), "scs_mlp_infer")
+    return out
+
+
+def save_model(path, params):
+    """Write a model file scs_load_model reads."""
+    p = np.ascontiguousarray(params, dtype=np.float32)
+    assert p.size == MLP_NPARAM
+    with open(path, "wb") as f:
+        f.write(b"SCSMLP01")
+        f.write(np.array([16, 128, 128, 1], dtype=np.uint32).tobytes())
+        f.write(p.tobytes())
+
+
+def load_model_file(path):
+    raw = open(path, "rb").read()
+    assert raw[:8] == b"SCSMLP01"
+    dims = np.frombuffer(raw[8:24], dtype=np.uint32)
+    assert list(dims) == [16, 128, 128, 1]
+    return np.frombuffer(raw[24:24 + 4 * MLP_NPARAM], dtype=np.float32).copy()
 
 
 _lib = None
@@ -104,6 +179,14 @@ def lib(build_if_missing=False):
     L.scs_debug_step.argtypes = [vp, C.c_uint32, _u32p, _u32p, _u64p, _u32p, _u32p,
                                  _u32p, _u32p, C.c_uint32, _u32p, C.c_uint64, _u32p,
                                  C.c_uint32]
+    fp = C.POINTER(C.c_float)
+    L.scs_load_model.argtypes = [vp, C.c_char_p]
+    L.scs_trace_enable.argtypes = [vp, C.c_uint64, C.c_uint32]
+    L.scs_trace_read.argtypes = [vp, fp, _u32p, C.c_uint64, _u64p]
+    L.scs_mlp_train.argtypes = [fp, fp, fp, C.c_uint64, C.POINTER(MlpTrainCfg), fp, fp, C.c_int]
+    L.scs_mlp_grad.argtypes = [fp, fp, fp, fp, C.c_uint64, C.POINTER(C.c_double), fp, C.c_int]
+    L.scs_mlp_infer.argtypes = [fp, fp, C.c_uint64, fp, C.c_int]
+    L.scs_mlp_last_error.restype = C.c_char_p
     _lib = L
     return L
 
@@ -307,6 +390,28 @@ class Engine:
             for r in rs:
                 got[r["ticket"]] = r
         return [got[t] for t in tickets]
+
+    def load_model(self, path):
+        """Use the network in model file `path` to pick branching vertices
+        (None: back to the plain method)."""
+        self._check(lib().scs_load_model(self._h, None if path is None else path.encode()),
+                    "scs_load_model")
+
+    def trace_enable(self, max_records, sample_shift=0):
+        self._check(lib().scs_trace_enable(self._h, max_records, sample_shift),
+                    "scs_trace_enable")
+        self._trace_cap = max_records
+
+    def trace_read(self):
+        """(features[k][16], keys[k][2] = (query tag, global vertex), records
+        produced incl. dropped ones)."""
+        cap = getattr(self, "_trace_cap", 0)
+        f = np.zeros((max(cap, 1), MLP_IN), dtype=np.float32)
+        k = np.zeros((max(cap, 1), 2), dtype=np.uint32)
+        w = C.c_uint64()
+        n = self._check(lib().scs_trace_read(self._h, _fp(f), _p(k), cap, C.byref(w)),
+                        "scs_trace_read")
+        return f[:n], k[:n], w.value
 
     def stats(self):
         arr = (C.c_uint64 * 20)()

@@ -213,3 +213,24 @@ def test_binding_structs_match_the_compiled_abi():
             E.Config.active_queries.offset, C.sizeof(E.Query), C.sizeof(E.Result),
             E.Result.nodes.offset, E.Result.search_ns.offset]
     assert out.tolist() == want
+
+
+def test_oracle_answers_match_reference_gpu_rows():
+    """The oracle's exact answers equal the reference's own GPU search
+    (its main.cu built unchanged, one query per server process, rows
+    recorded by tests/golden/make_ref_gpu.py) on every query of the
+    4000-vertex workload that the reference answered (Overtime = 0)."""
+    ref = json.load(open(os.path.join(GOLD, "ref_gpu_chunglu_n4000.json")))
+    gold = json.load(open(os.path.join(GOLD, "answers_chunglu_n4000.json")))
+    assert ref["checksum"] == gold["checksum"]
+    by_q = {(g["l"], g["h"], g["q"]): g for g in gold["queries"]}
+    compared = 0
+    for rq in ref["queries"]:
+        g = by_q[(rq["l"], rq["h"], rq["q"])]
+        for run in rq["runs"]:
+            if run.get("degree") is None or run.get("overtime") != 0:
+                continue
+            assert g["finished"]
+            assert run["degree"] == g["degree"], (rq, g)
+            compared += 1
+    assert compared >= 5

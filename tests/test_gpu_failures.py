@@ -56,24 +56,26 @@ def test_bad_queries_are_rejected_not_fatal(chunglu_small):
 
 
 def test_small_task_store_answers_match_golden(chunglu_small):
-    """A task store far smaller than the default (32k-word stacks per CTA, a
-    16 MB pool) on the 4000-vertex workload's queries the oracle solved
-    exactly: records spill from the stacks to the pool, the bottom records
-    are donated to idle CTAs and stolen, stacks slide down over the room the
-    donations left, and every answer still equals the golden one
-    (the reference's overflow store, src/helpers.cc:1393-1618)."""
+    """A task store far smaller than the default (64k-word stacks per CTA,
+    about eight of the largest task records; a 512 MB pool) on the
+    4000-vertex workload's queries the oracle solved exactly: records spill
+    from the stacks to the pool, the bottom records are donated to idle CTAs
+    and stolen, stacks slide down over the room the donations left, and
+    every answer still equals the golden one (the reference's overflow
+    store, src/helpers.cc:1393-1618)."""
     from scs_gb300.engine import DONE, HEURISTIC, Engine
     g = json.load(open(os.path.join(GOLD, "answers_chunglu_n4000.json")))["queries"]
     gold = [q for q in g if q["finished"] and not q["heu_hit"]]
     assert len(gold) >= 20
     rows = [(q["l"], q["h"], q["q"], q["heur"], q["limit_doms"]) for q in gold]
-    eng = Engine(graph=chunglu_small, limit_queries=16, stack_words=1 << 15,
-                 pool_words=1 << 22, slice_us=50000, active_queries=4)
+    eng = Engine(graph=chunglu_small, limit_queries=16, stack_words=1 << 16,
+                 pool_words=1 << 27, slice_us=50000, active_queries=4)
     try:
         res = eng.solve(rows)
         st = eng.stats()
     finally:
         eng.close()
+    print("small store:", {k: st[k] for k in ("spills", "donations", "steals", "slides")})
     for q, r in zip(gold, res):
         assert r["status"] in (DONE, HEURISTIC), (q, r)
         assert r["degree"] == q["degree"], (q, r)

@@ -271,3 +271,24 @@ def test_submit_from_many_threads_while_stepping(chunglu_small):
         g = gold[tickets[t]]
         assert r["status"] in (0, 1), r
         assert r["degree"] == g["degree"], (g, r)
+
+
+def test_engine_matches_reference_gpu_rows(eng_c1):
+    """The engine's answers equal the reference's own GPU search (main.cu
+    built unchanged and run one query per server process; rows in
+    tests/golden/ref_gpu_chunglu_n4000.json) on every query the reference
+    answered, and are never below a row it reported."""
+    ref = json.load(open(os.path.join(GOLD, "ref_gpu_chunglu_n4000.json")))
+    rows = [(q["l"], q["h"], q["q"], q["heur"], q["limit_doms"]) for q in ref["queries"]]
+    res = eng_c1.solve(rows)
+    answered = 0
+    for q, r in zip(ref["queries"], res):
+        assert r["status"] in (0, 1), r
+        for run in q["runs"]:
+            if run.get("degree") is None:
+                continue
+            assert r["degree"] >= run["degree"], (q, r)
+            if run["overtime"] == 0:
+                assert r["degree"] == run["degree"], (q, r)
+                answered += 1
+    assert answered >= 5

@@ -1,0 +1,125 @@
+"""The learned branching path on the GPU: the trace the exact solver emits,
+answers that do not depend on the network (any network, trained or not),
+and what the trained network gains over the plain method on held-out
+queries."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+MODEL = os.path.join(ROOT, "scs_gb300", "weights", "rmat_s15_ef16.mlp")
+
+
+def _gold_c1():
+    g = json.load(open(os.path.join(GOLD, "answers_chunglu_n4000.json")))["queries"]
+    return [q for q in g if q["finished"]]
+
+
+def _engine(graph, **kw):
+    from scs_gb300.engine import Engine
+    kw.setdefault("pool_words", 1 << 26)
+    kw.setdefault("stack_words", 1 << 22)
+    kw.setdefault("slice_us", 50000)
+    return Engine(graph=graph, **kw)
+
+
+def test_trace_records_shortlisted_candidates(chunglu_small):
+    """With the trace on, sampled steps record up to 16 candidates each: 16
+    finite features in their stated ranges, keyed by the query's tag (its
+    ticket) and a global vertex id of the graph."""
+    gold = _gold_c1()[:8]
+    rows = [(g["l"], g["h"], g["q"], g["heur"], g["limit_doms"]) for g in gold]
+    e = _engine(chunglu_small, limit_queries=16)
+    try:
+        e.trace_enable(200000, 0)
+        tickets = e.submit_many(rows)
+        e.run()
+        res = {r["ticket"]: r for r in e.poll()}
+        X, keys, produced = e.trace_read()
+    finally:
+        e.close()
+    assert len(X) > 0 and produced >= len(X)
+    assert np.isfinite(X).all()
+    tags = {t & 0xFFFFFFFF for t in tickets}
+    assert set(keys[:, 0].tolist()) <= tags
+    assert (keys[:, 1] < 4000).all()
+    assert (X[:, 0] >= 0).all() and (X[:, 0] <= 1).all()   # dC / |C|
+    assert set(np.unique(X[:, 8]).tolist()) <= {0.0, 1.0}   # rule's u* flag
+    assert (X[:, 7] <= 1.0 + 1e-6).all()                    # score / best score
+    # every traced step holds the rule's own u*
+    assert X[:, 8].sum() > 0
+    for t in tickets:
+        assert res[t]["status"] in (0, 1)
+
+
+def test_any_network_keeps_the_answers(chunglu_small, tmp_path):
+    """The network only picks u* among the candidates the reference's rule
+    accepts, so even an untrained network leaves every answer equal to the
+    exact one (the oracle's, recorded in tests/golden)."""
+    from oracle import mlp_ref as R
+    from scs_gb300.engine import save_model
+    path = str(tmp_path / "random.mlp")
+    save_model(path, R.init_params(21))
+    gold = _gold_c1()
+    rows = [(g["l"], g["h"], g["q"], g["heur"], g["limit_doms"]) for g in gold]
+    e = _engine(chunglu_small, limit_queries=64)
+    try:
+        e.load_model(path)
+        res = e.solve(rows)
+        e.load_model(None)
+        plain = e.solve(rows[:6])
+    finally:
+        e.close()
+    for g, r in zip(gold, res):
+        assert r["status"] in (0, 1), r
+        assert r["degree"] == g["degree"], (g, r)
+        if r["status"] == 0 and r["degree"] > g["kl_heu"]:
+            assert r["h_verified"] == 1
+    for g, r in zip(gold, plain):
+        assert r["degree"] == g["degree"]
+
+
+def test_bad_model_files_are_rejected(chunglu_small, tmp_path):
+    from scs_gb300.engine import SCSError
+    bad = tmp_path / "bad.mlp"
+    bad.write_bytes(b"SCSMLP01" + np.array([16, 64, 64, 1], np.uint32).tobytes())
+    e = _engine(chunglu_small, limit_queries=4)
+    try:
+        with pytest.raises(SCSError):
+            e.load_model(str(bad))
+        with pytest.raises(SCSError):
+            e.load_model(str(tmp_path / "missing.mlp"))
+        assert e.solve([(3, 6, 10, 1, 1)])[0]["status"] in (0, 1)
+    finally:
+        e.close()
+
+
+@pytest.mark.skipif(not os.path.exists(MODEL), reason="trained model not present")
+def test_trained_network_gain_on_heldout_queries():
+    """The trained network (scs_gb300/weights, trained by scs_gb300.train on
+    the exact solver's traces) against the plain method on 200 held-out
+    queries of the mid-size R-MAT workload (query seed 200), same 100k-task
+    budget: every query both solve exactly gets the same degree, and the
+    gain (exact answers, search tasks) is printed."""
+    from scs_gb300 import workloads as W
+    from scs_gb300.engine import Engine, core_numbers
+    from scs_gb300.train import HELDOUT_SEED, evaluate
+    n, u, v = W.rmat(15, 16 << 15)
+    off, adj = W.to_csr(n, u, v)
+    core = core_numbers(n, off, adj)
+    rows = [tuple(int(x) for x in r) for r in W.queries_mid(core, 200, seed=HELDOUT_SEED)]
+    e = Engine(csr=(n, off, adj), limit_queries=200, node_budget=100000)
+    try:
+        ev = evaluate(e, rows, MODEL)
+    finally:
+        e.close()
+    p, l = ev["plain"], ev["learned"]
+    print("plain exact %d tasks %d %.2fs | learned exact %d tasks %d %.2fs"
+          % (p["exact"], p["nodes"], p["seconds"], l["exact"], l["nodes"], l["seconds"]))
+    assert ev["agree_where_both_exact"] == ev["both_exact"]
+    # the learned path must answer at least as many queries exactly
+    assert l["exact"] >= p["exact"]
