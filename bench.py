@@ -46,6 +46,7 @@ sys.path.insert(0, ROOT)
 METRIC = "exact queries/sec + p50/p99 latency"
 UNIT = "queries/s"
 WORKLOAD = "rmat_s15_ef16_q1000"
+MODEL = os.path.join(ROOT, "scs_gb300", "weights", "rmat_s15_ef16.mlp")
 
 
 def env_rank():
@@ -182,7 +183,7 @@ def cpu_baseline(n, off, adj, rows, budget, procs=None, cap_s=0.0):
 
 def _cpu_desc(r, budget):
     t = np.array(r["times"]) if r["times"] else np.zeros(1)
-    return ("%d queries of the step (its first ones), one per process on %d host cores, "
+    return ("%d queries (the first of each step), one per process on %d host cores, "
             "node budget %d per query, no wall-clock cap; makespan %.1f s; %d exact, %d stopped "
             "by the budget; single-thread %.2f s per query (mean), %.0f tasks/s per core"
             % (r["queries"], r["procs"], budget, r["span_s"], r["exact"], r["budget_stopped"],
@@ -216,10 +217,13 @@ def _cpu_solve(args):
 
 def run_reference(args):
     """--impl reference: the reference's CPU path on the host cores, on the
-    same workload, metric and node budget as the GPU arm.  Each step times a
-    sample of the step's queries (its first --ref-sample) on all host cores;
-    value = exact answers / measured makespan.  Warm-up steps run a few other
-    queries (seed 43) under a small budget, only to start the processes."""
+    same workload, metric and node budget as the GPU arm.  Each of the K
+    timed steps contributes a sample of its own queries (its first
+    --ref-sample); the K samples run together on all host cores, one query
+    per process at a time, and the timed region is their makespan, so
+    ms_per_step = makespan / K and value = exact answers / makespan.
+    Warm-up steps run a few other queries (seed 43) under a small budget,
+    only to start the processes."""
     rank, world, _ = env_rank()
     if rank != 0:
         return 0
@@ -227,34 +231,33 @@ def run_reference(args):
     import oracle as O
     og = O.OracleGraph(n, off, adj)
     rows = queries_for(og.core, args.batch * args.steps, 42)
-    warm = queries_for(og.core, 8 * max(args.warmup, 1), 43)
     procs = os.cpu_count() or 1
-    for i in range(args.warmup):
-        cpu_baseline(n, off, adj, warm[i * 8:(i + 1) * 8], 1000, procs=procs)
-    spans, exact, total, last = 0.0, 0, 0, None
-    for i in range(args.steps):
-        step_rows = rows[i * args.batch:(i + 1) * args.batch][: args.ref_sample]
-        r = cpu_baseline(n, off, adj, step_rows, args.node_budget, procs=procs)
-        spans += r["span_s"]
-        exact += r["exact"]
-        total += r["queries"]
-        last = r
-    v = exact / spans if spans > 0 else 0.0
-    t = np.array(last["times"])
+    if args.warmup:
+        warm = queries_for(og.core, 2 * args.warmup, 43)
+        cpu_baseline(n, off, adj, warm, 1000, procs=procs)
+    sample = [r for i in range(args.steps)
+              for r in rows[i * args.batch:(i + 1) * args.batch][: args.ref_sample]]
+    r = cpu_baseline(n, off, adj, sample, args.node_budget, procs=procs)
+    span = r["span_s"]
+    v = r["exact"] / span if span > 0 else 0.0
+    t = np.array(r["times"])
     info = host_cpu_info()
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * spans / args.steps,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * span / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
             "data": "synthetic",
             "config": {"workload": WORKLOAD, "batch": args.batch, "sample_per_step": args.ref_sample,
-                       "node_budget": args.node_budget, "wall_cap": None,
-                       "all_answers_per_s": total / spans if spans > 0 else 0.0,
-                       "exact_fraction": exact / max(total, 1),
-                       "single_thread_s_per_query": float(t.mean()),
-                       "single_thread_exact_per_s": last["exact"] / max(float(t.sum()), 1e-9),
+                       "sampled_queries": len(sample), "node_budget": args.node_budget,
+                       "wall_cap": None,
+                       "timed_region": "the K steps' samples run together on all host cores "
+                                       "(makespan); ms_per_step = makespan / K",
+                       "all_answers_per_s": len(sample) / span if span > 0 else 0.0,
+                       "exact_fraction": r["exact"] / max(len(sample), 1),
+                       "single_thread_s_per_query": float(t.mean()) if len(t) else None,
+                       "single_thread_exact_per_s": r["exact"] / max(float(t.sum()), 1e-9),
                        **info},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": last["procs"], "kind": "port",
-                             "sample": _cpu_desc(last, args.node_budget)},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": r["procs"], "kind": "port",
+                             "sample": _cpu_desc(r, args.node_budget)},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
@@ -326,10 +329,19 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--batch", type=int, default=1000)
     ap.add_argument("--warmup-batch", type=int, default=48)
-    ap.add_argument("--node-budget", type=int, default=100000)
+    ap.add_argument("--node-budget", type=int, default=20000,
+                    help="search tasks per query (both arms); the stand-in for the "
+                         "reference's level cap")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--ref-sample", type=int, default=32,
-                    help="--impl reference: queries of each step timed on the host cores")
+    ap.add_argument("--arm", default="auto", choices=["auto", "plain", "learned"],
+                    help="learned: u* and an incumbent proposal from the trained network; "
+                         "plain: the integer rules alone; auto: learned when the model exists")
+    ap.add_argument("--model", default=MODEL, help="model file of the learned arm")
+    ap.add_argument("--no-compare", action="store_true",
+                    help="skip the other arm's run on the first step's queries")
+    ap.add_argument("--ref-sample", type=int, default=4,
+                    help="--impl reference: queries of each step timed on the host cores "
+                         "(all steps' samples run together)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ctas-per-sm", type=int, default=0,
                     help="search CTAs per SM (0: autotuned on the warm-up queries)")
@@ -380,6 +392,11 @@ def main():
                  node_budget=args.node_budget, stack_words=tune["stack_words"],
                  pool_words=args.pool_words, device=local,
                  active_queries=tune["active_queries"], release_order=args.release_order)
+    arm = args.arm
+    if arm == "auto":
+        arm = "learned" if os.path.exists(args.model) else "plain"
+    if arm == "learned":
+        eng.load_model(args.model)
     # weak scaling: every rank runs the full 1,000-query workload of its own
     # query seed (rank 0 uses the workload's seed 42)
     rows = queries_for(core, args.batch * args.steps, 42 + 1000 * rank)
@@ -415,6 +432,36 @@ def main():
     barrier()
     ck = clocks.stop(local)
     st1 = eng.stats()
+    compare = None
+    if not args.no_compare and (arm == "learned" or os.path.exists(args.model)):
+        # the other arm on the first step's queries (after the timed region)
+        other = "plain" if arm == "learned" else "learned"
+        eng.load_model(args.model if other == "learned" else None)
+        batch = [tuple(int(x) for x in r) for r in rows[: args.batch]]
+        flush_l2(torch, flush)
+        torch.cuda.synchronize()
+        s0 = eng.stats()
+        t0 = time.perf_counter()
+        oth = eng.solve(batch)
+        dt = time.perf_counter() - t0
+        s1 = eng.stats()
+        mine = results[: args.batch]
+        ex = lambda r: r["status"] in (0, 1)
+        both = [(a, b) for a, b in zip(mine, oth) if ex(a) and ex(b)]
+        lat_o = np.array([r["latency_ns"] for r in oth]) / 1e6
+        compare = {"arm": other, "queries": len(oth), "seconds": dt,
+                   "exact_per_s": sum(1 for r in oth if ex(r)) / dt,
+                   "all_answers_per_s": len(oth) / dt,
+                   "exact_fraction": sum(1 for r in oth if ex(r)) / max(len(oth), 1),
+                   "p50_ms": float(np.percentile(lat_o, 50)),
+                   "p99_ms": float(np.percentile(lat_o, 99)),
+                   "nodes": s1["nodes"] - s0["nodes"],
+                   "this_arm_exact_on_these": sum(1 for r in mine if ex(r)),
+                   "both_exact": len(both),
+                   "same_degree_where_both_exact": sum(1 for a, b in both
+                                                       if a["degree"] == b["degree"]),
+                   "degree_differs_anywhere_exact": sum(
+                       1 for a, b in zip(mine, oth) if ex(a) and ex(b) and a["degree"] != b["degree"])}
     # max of the times over ranks, sum of the queries
     t_dev, wall, total_q = reduce_over_ranks(dist, torch, dev_ms / 1e3, wall, len(results),
                                              "cuda")
@@ -458,7 +505,10 @@ def main():
                    "resident_ctas": st1["ctas"], "smem_state_words": st1["smem_words"],
                    "active_queries": st1["active"],
                    "slice_us": tune["slice_us"], "stack_words": tune["stack_words"],
-                   "autotune_trials": trials},
+                   "autotune_trials": trials,
+                   "arm": arm, "model": os.path.relpath(args.model, ROOT) if arm == "learned" else None,
+                   "proposals_better": st1["proposals_better"] - st0["proposals_better"],
+                   "compare": compare},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak if peak else None, "traffic": traffic,
                      "peak_kind": peak_kind, "kernel": "search_kernel",

@@ -74,6 +74,13 @@ typedef struct {
   uint32_t release_order;     /* which prepared query is searched next:
                                  0 the smallest local graph (shortest job
                                  first), 1 admission order */
+  uint32_t release_headroom;  /* admission by free task-store memory: a
+                                 prepared query is released to the search
+                                 only while the shared pool has room for this
+                                 many records of its root's size beyond what
+                                 earlier releases of the slice claimed
+                                 (0: 4).  When nothing is being searched the
+                                 next query is released regardless. */
 } scs_config;
 
 /* One query: the reference's message fields (main.cu:92-119). */
@@ -138,7 +145,7 @@ int scs_poll(scs_engine *e, scs_result *out, int max, uint32_t *h_buf,
              uint32_t h_stride);
 
 /* Engine counters (array of SCS_STAT_COUNT u64). */
-#define SCS_STAT_COUNT 20
+#define SCS_STAT_COUNT 24
 enum {
   SCS_STAT_NODES = 0,     /* tasks processed */
   SCS_STAT_SLICES = 1,    /* search slices launched */
@@ -164,8 +171,11 @@ enum {
   SCS_STAT_RELEASES = 17, /* prepared queries released to the search */
   SCS_STAT_SLIDES = 18,   /* task-stack slides: a CTA's live records moved
                              down over the room donations left below them */
-  SCS_STAT_PROPOSALS_BETTER = 19 /* learned incumbent proposals that raised
+  SCS_STAT_PROPOSALS_BETTER = 19, /* learned incumbent proposals that raised
                              a query's incumbent (model loaded) */
+  SCS_STAT_HELD_MEMORY = 20, /* slices in which a prepared query waited for
+                             pool room (release_headroom) */
+  SCS_STAT_POOL_FREE = 21  /* shared-pool words free after the last slice */
 };
 int scs_stats(scs_engine *e, uint64_t *out);
 

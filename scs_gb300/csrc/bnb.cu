@@ -1228,6 +1228,7 @@ __device__ void learned_choice(const SearchParams &P, Task &T, Sh &sh) {
   __syncthreads();
 }
 
+template <bool LRN>
 __device__ void choose_ustar(const SearchParams &P, Task &T, Sh &sh) {
   const int t = threadIdx.x;
   const uint32_t s = sh.s;
@@ -1312,7 +1313,7 @@ __device__ void choose_ustar(const SearchParams &P, Task &T, Sh &sh) {
       }
     }
   }
-  if (sh.lrn) shortlist(best, bid, bpos, sh);  // read after block_argmax's barriers
+  if (LRN && sh.lrn) shortlist(best, bid, bpos, sh);  // read after block_argmax's barriers
   double osc;
   uint32_t oid;
   block_argmax(best, bid, sh, osc, oid);
@@ -1324,7 +1325,7 @@ __device__ void choose_ustar(const SearchParams &P, Task &T, Sh &sh) {
     if (SCS_PROF_MODE == 3) sh.sub[2] += clock64() - c0;
   }
   __syncthreads();
-  if (sh.lrn && sh.ustar != UINT32_MAX) learned_choice(P, T, sh);
+  if (LRN && sh.lrn && sh.ustar != UINT32_MAX) learned_choice(P, T, sh);
 }
 
 // reset the pushed scores (candidates are exactly the R vertices with C
@@ -1697,6 +1698,7 @@ __device__ void clear_aux_list(Task &T, Sh &sh) {
 // one step on the loaded task (phases up to the choice of u* and doms)
 // returns outcome in sh.outcome
 // ---------------------------------------------------------------------------
+template <bool LRN>
 __device__ void step_core(const SearchParams &P, Task &T, Sh &sh, bool test,
                           uint32_t *t_wit) {
   const int t = threadIdx.x;
@@ -1748,7 +1750,7 @@ __device__ void step_core(const SearchParams &P, Task &T, Sh &sh, bool test,
     __syncthreads();
     return;
   }
-  choose_ustar(P, T, sh);
+  choose_ustar<LRN>(P, T, sh);
   phase_mark(sh, 4);
   if (sh.ustar == UINT32_MAX) {
     clear_scores(T, sh);
@@ -1851,7 +1853,7 @@ step_test_kernel(SearchParams P) {
   __syncthreads();
   load_record(rec, T, sh);
   uint32_t *wit = P.t_wit + (size_t)ti * P.t_wit_stride;
-  step_core(P, T, sh, true, wit);
+  step_core<false>(P, T, sh, true, wit);
   uint32_t *hdr = P.t_hdr + 16 * ti;
   uint32_t *kids = P.t_kids + (size_t)ti * P.t_kids_stride;
   if (sh.outcome == 0) {
@@ -2034,8 +2036,11 @@ __device__ void stack_make_room(const SearchParams &P, uint32_t *sbase,
   __syncthreads();
 }
 
-__global__ void __launch_bounds__(BT, SEARCH_MINB)
-search_kernel(SearchParams P) {
+// The persistent search; LRN adds the learned branching choice and the
+// trace (two kernels, so the plain one carries none of that code and keeps
+// its registers for the step itself).
+template <bool LRN>
+__device__ __forceinline__ void search_body(const SearchParams &P) {
   extern __shared__ uint32_t dyn[];
   __shared__ Sh sh;
   __shared__ unsigned long long s_top, s_bot;
@@ -2205,7 +2210,7 @@ search_kernel(SearchParams P) {
     const uint32_t s_in = sh.s;
     const unsigned long long c_step = clock64();
 #endif
-    step_core(P, T, sh, false, nullptr);
+    step_core<LRN>(P, T, sh, false, nullptr);
 #if SCS_PROF_MODE == 2
     if (t == 0) {
       const int b = s_in < 512 ? 0 : s_in < 4096 ? 1 : 2;
@@ -2412,6 +2417,16 @@ search_kernel(SearchParams P) {
       atomicAdd(&P.ctr->sub_counts[i], sh.cnt4[i]);
     }
   }
+}
+
+__global__ void __launch_bounds__(BT, SEARCH_MINB)
+search_kernel(SearchParams P) {
+  search_body<false>(P);
+}
+
+__global__ void __launch_bounds__(BT, SEARCH_MINB)
+search_kernel_learned(SearchParams P) {
+  search_body<true>(P);
 }
 
 }  // namespace scs

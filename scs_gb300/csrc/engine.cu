@@ -117,6 +117,7 @@ struct scs_engine {
   uint32_t n_parked = 0;
   uint32_t *d_rel = nullptr;
   uint32_t active_target = 0;
+  unsigned long long pool_free = ~0ull;  // pool words free after the last slice
   Scratch scr{};
   Counters *d_ctr = nullptr;
   uint32_t rules = 31;
@@ -301,15 +302,23 @@ static int engine_init(scs_engine *E) {
   size_t words = budget > stat ? (budget - stat) / 4 : 0;
   E->nw_smem = (uint32_t)std::min<size_t>(words, std::min<uint32_t>(n, MAX_LOCAL));
   E->smem_bytes = (size_t)E->nw_smem * 4;
-  CK(cudaFuncSetAttribute(search_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                          (int)E->smem_bytes));
-  CK(cudaFuncSetAttribute(search_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
-                          (int)cudaSharedmemCarveoutMaxShared));
+  for (const void *k : {(const void *)search_kernel, (const void *)search_kernel_learned}) {
+    CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)E->smem_bytes));
+    CK(cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout,
+                            (int)cudaSharedmemCarveoutMaxShared));
+  }
   CK(cudaFuncSetAttribute(step_test_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                           (int)E->smem_bytes));
   int occ = 0;
   CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, search_kernel, SEARCH_THREADS,
                                                    E->smem_bytes));
+  {
+    int occ_l = 0;  // the learned variant must fit the same grid
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_l, search_kernel_learned,
+                                                     SEARCH_THREADS, E->smem_bytes));
+    occ = std::min(occ, occ_l);
+  }
   if (occ < 1) {
     E->err = "search kernel does not fit on an SM";
     return SCS_ECUDA;
@@ -354,6 +363,7 @@ static int engine_init(scs_engine *E) {
   RC(E->dalloc(&E->pool.arena_top, 1));
   // the bump area starts after the parked roots
   CK(cudaMemcpyAsync(E->pool.arena_top, &E->root_words, 8, cudaMemcpyHostToDevice, E->stream));
+  E->pool_free = pw;
   RC(E->dalloc(&E->d_rel, E->nslots, false));
   // Queries searched at once.  Fewer keep the active local graphs in L2 (the
   // search is bound by dependent loads); enough must stay to feed every CTA
@@ -590,11 +600,27 @@ static int slice(scs_engine *E) {
           return E->h_slots[a].n_local < E->h_slots[b].n_local;
         });
       }
+      // Admission by free task-store memory: each released query claims
+      // release_headroom records of its root's size from the pool's free
+      // words (read back after the last slice).  With nothing searched, one
+      // query goes regardless, so the engine always progresses.
+      const unsigned long long head = E->cfg.release_headroom ? E->cfg.release_headroom : 4;
+      unsigned long long budget = E->pool_free;
+      bool held = false;
       for (uint32_t i = 0; i < cand.size() && rel.size() < need; i++) {
+        const uint32_t nl = E->h_slots[cand[i]].n_local;
+        const unsigned long long claim =
+            head * (2ull * (nl ? nl : std::min<uint32_t>(E->g.n, MAX_LOCAL)) + 5);
+        if (claim > budget && !(active == 0 && rel.empty())) {
+          held = true;
+          break;
+        }
+        budget -= std::min(budget, claim);
         E->slots[cand[i]].parked = false;
         E->n_parked--;
         rel.push_back(cand[i]);
       }
+      if (held) E->stats[SCS_STAT_HELD_MEMORY]++;
       std::deque<uint32_t> keep;
       for (uint32_t si : E->parked)
         if (E->slots[si].parked) keep.push_back(si);
@@ -617,11 +643,14 @@ static int slice(scs_engine *E) {
   // done_count, stop
   CK(cudaMemsetAsync(&E->d_ctr->deadline, 0, 8, E->stream));
   CK(cudaMemsetAsync(&E->d_ctr->hungry, 0, sizeof(uint32_t) * 4, E->stream));
+  // the learned variant when a model is loaded or the trace is on
+  void (*kern)(SearchParams) =
+      (E->learned || E->trace_cap) ? search_kernel_learned : search_kernel;
   // the dynamic shared-memory limit is per function, not per engine
-  CK(cudaFuncSetAttribute(search_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                           (int)E->smem_bytes));
   CK(cudaEventRecord(E->ev0, E->stream));
-  search_kernel<<<E->grid, SEARCH_THREADS, E->smem_bytes, E->stream>>>(P);
+  kern<<<E->grid, SEARCH_THREADS, E->smem_bytes, E->stream>>>(P);
   CK(cudaGetLastError());
   CK(cudaEventRecord(E->ev1, E->stream));
   E->stats[SCS_STAT_LAUNCHES]++;
@@ -700,15 +729,18 @@ static int slice(scs_engine *E) {
   // pool reset when fully drained: every published record taken, and
   // something allocated (failed reservations also advance arena_top, so a
   // full arena with nothing published is reset too)
+  E->pool_free = E->pool.arena_cap > arena_used ? E->pool.arena_cap - arena_used : 0;
   if (ph[0] >= std::min(ph[1], E->pool.desc_cap) && (ph[1] > 0 || arena_used > E->root_words)) {
     uint32_t used = std::min(ph[1], E->pool.desc_cap);
     CK(cudaMemsetAsync(E->pool.desc, 0, used * 8ull, E->stream));
     // the bump area restarts after the parked roots, which stay in place
     CK(cudaMemcpyAsync(E->pool.arena_top, &E->root_words, 8, cudaMemcpyHostToDevice,
                        E->stream));
+    E->pool_free = E->pool.arena_cap - E->root_words;
     CK(cudaMemsetAsync(E->pool.head, 0, 4, E->stream));
     CK(cudaMemsetAsync(E->pool.tail, 0, 4, E->stream));
   }
+  E->stats[SCS_STAT_POOL_FREE] = E->pool_free;
   CK(cudaStreamSynchronize(E->stream));
   return 0;
 }

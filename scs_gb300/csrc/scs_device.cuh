@@ -227,6 +227,8 @@ __global__ void prep_kernel(DevGraph g, SlotArrays sa, Slot *slots,
                             const PrepJob *jobs, int njobs, PrepScratch ps,
                             Pool pool, Counters *ctr);
 __global__ void search_kernel(SearchParams P);
+// the same search with the learned branching choice and the trace
+__global__ void search_kernel_learned(SearchParams P);
 __global__ void release_kernel(Slot *slots, const uint32_t *cand, uint32_t n,
                                unsigned long long root_stride, Pool pool,
                                Counters *ctr);

@@ -24,7 +24,7 @@ STATUS_NAMES = {DONE: "done", HEURISTIC: "heuristic", CAPACITY: "capacity",
 STAT_NAMES = ["nodes", "slices", "donations", "steals", "spills", "bytes",
               "prep_bytes", "search_ns", "prep_ns", "launches", "h2d_bytes",
               "d2h_bytes", "heur_ns", "ctas", "smem_words", "errors", "active",
-              "releases", "slides", "proposals_better"]
+              "releases", "slides", "proposals_better", "held_memory", "pool_free"]
 
 
 class Config(C.Structure):
@@ -36,7 +36,7 @@ class Config(C.Structure):
                 ("pool_words", C.c_uint64), ("slice_us", C.c_uint32),
                 ("node_budget", C.c_uint64), ("host_threads", C.c_uint32),
                 ("device", C.c_int32), ("active_queries", C.c_uint32),
-                ("release_order", C.c_uint32)]
+                ("release_order", C.c_uint32), ("release_headroom", C.c_uint32)]
 
 
 class Query(C.Structure):
@@ -306,7 +306,7 @@ class Engine:
     def __init__(self, graph=None, csr=None, limit_queries=64, rules=None,
                  slice_us=0, node_budget=0, ctas_per_sm=0, stack_words=0,
                  pool_words=0, host_threads=0, device=0, active_queries=0,
-                 release_order=0):
+                 release_order=0, release_headroom=0):
         L = lib()
         cfg = Config()
         cfg.limit_queries = limit_queries
@@ -319,6 +319,7 @@ class Engine:
         cfg.device = device
         cfg.active_queries = active_queries
         cfg.release_order = release_order
+        cfg.release_headroom = release_headroom
         if rules is not None:
             cfg.rules_set = 1
             cfg.red1, cfg.red2, cfg.red3, cfg.prun1, cfg.prun2 = [int(bool(r)) for r in rules]
@@ -414,7 +415,7 @@ class Engine:
         return f[:n], k[:n], w.value
 
     def stats(self):
-        arr = (C.c_uint64 * 20)()
+        arr = (C.c_uint64 * 24)()
         self._check(lib().scs_stats(self._h, arr), "scs_stats")
         return {name: int(arr[i]) for i, name in enumerate(STAT_NAMES)}
 

@@ -56,8 +56,8 @@ def test_bad_queries_are_rejected_not_fatal(chunglu_small):
 
 
 def test_small_task_store_answers_match_golden(chunglu_small):
-    """A task store far smaller than the default (64k-word stacks per CTA,
-    about eight of the largest task records; a 512 MB pool) on the
+    """A task store far smaller than the default (16k-word stacks per CTA,
+    two of the largest task records; a 512 MB pool) on the
     4000-vertex workload's queries the oracle solved exactly: records spill
     from the stacks to the pool, the bottom records are donated to idle CTAs
     and stolen, stacks slide down over the room the donations left, and
@@ -68,7 +68,7 @@ def test_small_task_store_answers_match_golden(chunglu_small):
     gold = [q for q in g if q["finished"] and not q["heu_hit"]]
     assert len(gold) >= 20
     rows = [(q["l"], q["h"], q["q"], q["heur"], q["limit_doms"]) for q in gold]
-    eng = Engine(graph=chunglu_small, limit_queries=16, stack_words=1 << 16,
+    eng = Engine(graph=chunglu_small, limit_queries=16, stack_words=1 << 14,
                  pool_words=1 << 27, slice_us=50000, active_queries=4)
     try:
         res = eng.solve(rows)
@@ -81,3 +81,26 @@ def test_small_task_store_answers_match_golden(chunglu_small):
         assert r["degree"] == q["degree"], (q, r)
     assert st["spills"] > 0 and st["donations"] > 0 and st["steals"] > 0, st
     assert st["slides"] > 0, st
+
+
+def test_release_waits_for_pool_room(chunglu_small):
+    """Admission by free task-store memory: with a pool that holds only a
+    few root-sized records, prepared queries wait for room (release_headroom
+    records of their root's size each) instead of all starting at once, and
+    every answer still equals the golden one."""
+    from scs_gb300.engine import DONE, HEURISTIC, Engine
+    g = json.load(open(os.path.join(GOLD, "answers_chunglu_n4000.json")))["queries"]
+    gold = [q for q in g if q["finished"] and not q["heu_hit"]][:16]
+    rows = [(q["l"], q["h"], q["q"], q["heur"], q["limit_doms"]) for q in gold]
+    eng = Engine(graph=chunglu_small, limit_queries=32, stack_words=1 << 22,
+                 pool_words=1 << 17, slice_us=20000, release_headroom=4)
+    try:
+        res = eng.solve(rows)
+        st = eng.stats()
+    finally:
+        eng.close()
+    for q, r in zip(gold, res):
+        assert r["status"] in (DONE, HEURISTIC), (q, r)
+        assert r["degree"] == q["degree"], (q, r)
+    assert st["held_memory"] > 0, st
+    assert st["releases"] == sum(1 for r in res if r["nodes"] > 0)
