@@ -45,7 +45,14 @@ sys.path.insert(0, ROOT)
 
 METRIC = "exact queries/sec + p50/p99 latency"
 UNIT = "queries/s"
-WORKLOAD = "rmat_s15_ef16_q1000"
+# --workload: graph name in scs_gb300.workloads, workload name, description
+WORKLOADS = {
+    "rmat_s15": ("rmat_s15_ef16", "rmat_s15_ef16_q1000", "R-MAT scale 15, 524288 edges"),
+    "chunglu_n1m": ("chunglu_n1m", "chunglu_n1m_q10000_uneven",
+                    "Chung-Lu n=1,000,000, m=20,000,000, exponent 2.3"),
+    "rmat_s22": ("rmat_s22_ef16", "rmat_s22_ef16_serving", "R-MAT scale 22, edge factor 16"),
+}
+_WL = ["rmat_s15"]
 MODEL = os.path.join(ROOT, "scs_gb300", "weights", "rmat_s15_ef16.mlp")
 
 
@@ -56,14 +63,16 @@ def env_rank():
 
 def build_workload(batch, warmup, steps):
     from scs_gb300 import workloads as W
-    n, u, v = W.rmat(15, 16 << 15)
+    gb, _ = W.WORKLOADS[WORKLOADS[_WL[0]][0]]
+    n, u, v = gb()
     off, adj = W.to_csr(n, u, v)
     return n, off, adj
 
 
 def queries_for(core, count, seed):
     from scs_gb300 import workloads as W
-    return W.queries_mid(core, count=count, seed=seed)
+    _, qb = W.WORKLOADS[WORKLOADS[_WL[0]][0]]
+    return qb(core, count=count, seed=seed)
 
 
 class Clocks:
@@ -246,7 +255,7 @@ def run_reference(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * span / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
             "data": "synthetic",
-            "config": {"workload": WORKLOAD, "batch": args.batch, "sample_per_step": args.ref_sample,
+            "config": {"workload": WORKLOADS[_WL[0]][1], "batch": args.batch, "sample_per_step": args.ref_sample,
                        "sampled_queries": len(sample), "node_budget": args.node_budget,
                        "wall_cap": None,
                        "timed_region": "the K steps' samples run together on all host cores "
@@ -280,10 +289,13 @@ def run_serve(args):
         rows = [tuple(int(x) for x in r) for r in queries_for(core, count, 44)]
         rng = np.random.default_rng(45)
         arrive = np.cumsum(rng.exponential(1.0 / rate, count))
-        eng = Engine(csr=(n, off, adj), limit_queries=256, slice_us=args.slice_us or 5000,
+        eng = Engine(csr=(n, off, adj), limit_queries=args.slots or 256,
+                     slice_us=args.slice_us or 5000,
                      ctas_per_sm=args.ctas_per_sm, node_budget=args.node_budget,
                      stack_words=args.stack_words, pool_words=args.pool_words, device=local,
-                     active_queries=args.active_queries)
+                     active_queries=args.active_queries, max_local=args.max_local)
+        if args.arm == "learned":
+            eng.load_model(args.model)
         eng.solve([tuple(int(x) for x in r) for r in queries_for(core, 8, 46)])  # warm-up
         pending, lat, res = {}, [], []
         i = 0
@@ -315,9 +327,11 @@ def run_serve(args):
                 "exact_fraction": sum(1 for r in res if r["status"] in (0, 1)) / max(len(res), 1),
                 "verified_fraction": sum(1 for r in res if r["h_verified"]) / max(len(res), 1),
                 "data": "synthetic",
-                "config": {"workload": WORKLOAD, "arrival_window_s": args.serve_seconds,
+                "config": {"workload": WORKLOADS[_WL[0]][1], "arrival_window_s": args.serve_seconds,
                            "node_budget": args.node_budget, "slice_us": args.slice_us or 5000,
-                           "active_queries": st["active"], "slots": 256}}
+                           "active_queries": st["active"], "slots": args.slots or 256,
+                           "arm": args.arm if args.arm != "auto" else "plain",
+                           "held_by_memory": st["held_memory"]}}
         print(json.dumps(line), flush=True)
     return 0
 
@@ -333,6 +347,14 @@ def main():
                     help="search tasks per query (both arms); the stand-in for the "
                          "reference's level cap")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="rmat_s15", choices=sorted(WORKLOADS),
+                    help="rmat_s15: the mid-size workload (default, the measured one); "
+                         "chunglu_n1m: uneven queries on the 1M-vertex Chung-Lu graph; "
+                         "rmat_s22: the scale-22 R-MAT serving workload")
+    ap.add_argument("--slots", type=int, default=0,
+                    help="query slots (0: the batch size, at most 1000)")
+    ap.add_argument("--max-local", type=int, default=0,
+                    help="largest local graph searched (0: the engine default)")
     ap.add_argument("--arm", default="auto", choices=["auto", "plain", "learned"],
                     help="learned: u* and an incumbent proposal from the trained network; "
                          "plain: the integer rules alone; auto: learned when the model exists")
@@ -361,6 +383,7 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=20.0,
                     help="serving mode: arrival window per rate (seconds)")
     args = ap.parse_args()
+    _WL[0] = args.workload
     if args.impl == "reference":
         return run_reference(args)
     if args.serve:
@@ -387,14 +410,15 @@ def main():
         from scs_gb300.autotune import autotune
         sample = [tuple(int(x) for x in r) for r in warm[: min(len(warm), 64)]]
         tune, trials = autotune(n, off, adj, sample, args.node_budget, device=local)
-    eng = Engine(csr=(n, off, adj), limit_queries=max(args.batch, 1),
+    eng = Engine(csr=(n, off, adj), limit_queries=args.slots or max(min(args.batch, 1000), 1),
                  slice_us=tune["slice_us"], ctas_per_sm=tune["ctas_per_sm"],
                  node_budget=args.node_budget, stack_words=tune["stack_words"],
                  pool_words=args.pool_words, device=local,
-                 active_queries=tune["active_queries"], release_order=args.release_order)
+                 active_queries=tune["active_queries"], release_order=args.release_order,
+                 max_local=args.max_local)
     arm = args.arm
-    if arm == "auto":
-        arm = "learned" if os.path.exists(args.model) else "plain"
+    if arm == "auto":  # the model is trained on the mid-size workload
+        arm = "learned" if os.path.exists(args.model) and args.workload == "rmat_s15" else "plain"
     if arm == "learned":
         eng.load_model(args.model)
     # weak scaling: every rank runs the full 1,000-query workload of its own
@@ -492,7 +516,7 @@ def main():
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * t_dev / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD, "graph": "R-MAT scale 15, 524288 edges",
+        "config": {"workload": WORKLOADS[_WL[0]][1], "graph": "R-MAT scale 15, 524288 edges",
                    "queries": total_q, "exact_answers": exact_all,
                    "all_answers_per_s": total_q / t_dev,
                    "batch": args.batch, "node_budget": args.node_budget,

@@ -49,7 +49,8 @@ extern "C" {
 #define SCS_TIMEOUT 3       /* stopped by the search budget: best found,
                                the reference's Overtime=1 (main.cu:444-463) */
 #define SCS_BAD_QUERY 4     /* malformed query (main.cu:106-109) */
-#define SCS_TOO_LARGE 5     /* filtered graph exceeds the engine's limits */
+#define SCS_TOO_LARGE 5     /* filtered graph exceeds the engine's limits
+                               (scs_config.max_local, 15-bit degrees) */
 
 /* Engine configuration.  Field meanings follow the reference CLI where one
  * exists (main.cu:476-502); zero selects the default. */
@@ -81,6 +82,14 @@ typedef struct {
                                  earlier releases of the slice claimed
                                  (0: 4).  When nothing is being searched the
                                  next query is released regardless. */
+  uint32_t max_local;         /* largest local (filtered) graph a query may
+                                 search, in vertices (0: min(n, 2^21)); larger
+                                 ones report SCS_TOO_LARGE.  Each search CTA
+                                 keeps about 13 words of scratch per vertex of
+                                 this size, and each slot a parked root of
+                                 2*max_local+5 words.  A local graph with a
+                                 vertex of more than 32,767 local neighbours
+                                 is too large at any setting. */
 } scs_config;
 
 /* One query: the reference's message fields (main.cu:92-119). */

@@ -230,6 +230,22 @@ __device__ __forceinline__ void warp_append(bool want, uint32_t val,
   if (want) dst[base + __popc(m & ((1u << lane) - 1u))] = val;
 }
 
+// The same, appending a pair (val to dst, val2 to dst2 at the same index).
+__device__ __forceinline__ void warp_append2(bool want, uint32_t val, uint32_t val2,
+                                             uint32_t *cnt, uint32_t *dst, uint32_t *dst2) {
+  const int lane = threadIdx.x & 31;
+  unsigned m = __ballot_sync(0xffffffffu, want);
+  if (!m) return;
+  uint32_t base = 0;
+  if (lane == __ffs(m) - 1) base = atomicAdd(cnt, __popc(m));
+  base = __shfl_sync(0xffffffffu, base, __ffs(m) - 1);
+  if (want) {
+    const uint32_t o = base + __popc(m & ((1u << lane) - 1u));
+    dst[o] = val;
+    dst2[o] = val2;
+  }
+}
+
 __device__ __forceinline__ void phase_mark(Sh &sh, int which) {
   // thread 0 only: charge the cycles since the last mark to phase `which`
   if (threadIdx.x == 0) {
@@ -249,6 +265,7 @@ struct Task {
   uint32_t *list2;  // second buffer for stable compaction
   uint32_t *aux;
   uint32_t *tmp;
+  uint32_t *cpos;  // list position of the candidate at the same index of tmp
   double *ssc;   // pushed ustar scores, by local id (zero between uses)
   unsigned long long *cmask;  // C-neighbour masks of the candidates, by local id
   uint32_t *bits;  // N[u*] as a bitmap in shared memory after W (null: aux)
@@ -1248,8 +1265,8 @@ __device__ void choose_ustar(const SearchParams &P, Task &T, Sh &sh) {
     for (int j = 0; j < SCS_LIST_UNROLL; j++) {
       const uint32_t i = i0 + BT * j + t;
       const bool c = x[j] != SENT && st_of(w[j]) == ST_R && dc_of(w[j]) > 0;
-      // candidates carry their list position: (i << 16) | x (both < 2^16)
-      warp_append(c, (i << 16) | (x[j] & 0xFFFFu), &sh.cnt[0], T.tmp);
+      // candidates carry their list position (cpos, same index)
+      warp_append2(c, x[j], i, &sh.cnt[0], T.tmp, T.cpos);
     }
   }
   __syncthreads();
@@ -1283,14 +1300,14 @@ __device__ void choose_ustar(const SearchParams &P, Task &T, Sh &sh) {
     uint32_t wv[SCS_ARGMAX_UNROLL];
 #pragma unroll
     for (int j = 0; j < SCS_ARGMAX_UNROLL; j++) {
-      const uint32_t x = pk[j] != SENT ? (pk[j] & 0xFFFFu) : 0u;
+      const uint32_t x = pk[j] != SENT ? pk[j] : 0u;
       mv[j] = reinterpret_cast<const unsigned long long *>(T.ssc)[x];
       wv[j] = T.W[x];
     }
 #pragma unroll
     for (int j = 0; j < SCS_ARGMAX_UNROLL; j++) {
       if (pk[j] == SENT) continue;
-      const uint32_t x = pk[j] & 0xFFFFu;
+      const uint32_t x = pk[j];
       double sc;
       if (masked) {
         unsigned long long m = mv[j];
@@ -1309,7 +1326,7 @@ __device__ void choose_ustar(const SearchParams &P, Task &T, Sh &sh) {
       if (sc > best || (sc == best && sc > 0.0 && x < bid)) {
         best = sc;
         bid = x;
-        bpos = pk[j] >> 16;
+        bpos = T.cpos[c0 + BT * j + t];
       }
     }
   }
@@ -1331,7 +1348,7 @@ __device__ void choose_ustar(const SearchParams &P, Task &T, Sh &sh) {
 // reset the pushed scores (candidates are exactly the R vertices with C
 // neighbours, i.e. every vertex that received a term)
 __device__ void clear_scores(Task &T, Sh &sh) {
-  for (uint32_t ci = threadIdx.x; ci < sh.ndom_cand; ci += BT) T.ssc[T.tmp[ci] & 0xFFFFu] = 0.0;
+  for (uint32_t ci = threadIdx.x; ci < sh.ndom_cand; ci += BT) T.ssc[T.tmp[ci]] = 0.0;
   __syncthreads();
 }
 
@@ -1366,17 +1383,17 @@ __device__ void find_doms(Task &T, Sh &sh) {
   const uint32_t nc = sh.ndom_cand;
   const double dmax = (double)sh.dmax;
   const bool root_c = sh.csize <= 1;  // dom partial sum is 0 when |C| == 1
-  uint32_t *dom_id = T.tmp + sh.s;  // second half of tmp (s <= n)
+  uint32_t *dom_id = T.tmp + sh.s;  // second half of tmp (s <= n): candidate indices
   // With masks: v's C neighbours must all be neighbours of u* (u* is in R),
   // so mask(v) within mask(u*) is necessary as well.
   const bool use_mask = sh.masked;
   const unsigned long long mu = use_mask ? T.cmask[u] : 0ull;
-  auto record = [&](uint32_t pk) {
-    const uint32_t x = pk & 0xFFFFu;
+  auto record = [&](uint32_t ci) {
+    const uint32_t x = T.tmp[ci];
     const double part = root_c ? 0.0 : T.ssc[x];
     const double sc = __dadd_rn(part, __ddiv_rn((double)dr_of(T.W[x]), dmax));
     const uint32_t k = atomicAdd(&sh.cnt[1], 1u);
-    dom_id[k] = pk;  // packed with the list position
+    dom_id[k] = ci;  // the candidate's index (id in tmp, position in cpos)
     T.dsc2[k] = sc;
   };
   // Stage 1, one thread per candidate: the prefilters and the first
@@ -1386,10 +1403,8 @@ __device__ void find_doms(Task &T, Sh &sh) {
   for (uint32_t i0 = 0; i0 < nc; i0 += BT) {
     const uint32_t ci = i0 + t;
     bool more = false;
-    uint32_t pk = 0;
     if (ci < nc) {
-      pk = T.tmp[ci];
-      const uint32_t x = pk & 0xFFFFu;
+      const uint32_t x = T.tmp[ci];
       const uint32_t wx = T.W[x];
       bool dom = x != u && dc_of(wx) <= dcu && dc_of(wx) + dr_of(wx) <= degu + 1u &&
                  !(use_mask && (T.cmask[x] & ~mu));
@@ -1410,11 +1425,11 @@ __device__ void find_doms(Task &T, Sh &sh) {
         }
         if (dom) {
           if (stop < e) more = true;
-          else record(pk);
+          else record(ci);
         }
       }
     }
-    warp_append(more, pk, &sh.cnt[2], undec);
+    warp_append(more, ci, &sh.cnt[2], undec);
   }
   __syncthreads();
 #if SCS_PROF_MODE == 5
@@ -1429,7 +1444,7 @@ __device__ void find_doms(Task &T, Sh &sh) {
     const int lane = t & 31, wid = t >> 5;
     const uint32_t nu = sh.cnt[2];
     for (uint32_t j = wid; j < nu; j += NWARP) {
-      const uint32_t pk = undec[j], x = pk & 0xFFFFu;
+      const uint32_t ci = undec[j], x = T.tmp[ci];
       const uint32_t e = T.off[x + 1];
       bool dom = true;
       for (uint32_t k0 = T.off[x] + SCS_LANE_DOM; k0 < e && dom; k0 += 32 * SCS_ROW_UNROLL) {
@@ -1445,7 +1460,7 @@ __device__ void find_doms(Task &T, Sh &sh) {
           bad |= nb[q] != SENT && live(T.W[nb[q]]) && !marked(nb[q]);
         dom = !__any_sync(0xffffffffu, bad);
       }
-      if (dom && lane == 0) record(pk);
+      if (dom && lane == 0) record(ci);
     }
   }
   __syncthreads();
@@ -1467,12 +1482,12 @@ __device__ void find_doms(Task &T, Sh &sh) {
     uint32_t bi = UINT32_MAX, bpos = UINT32_MAX, bli = 0;
     for (uint32_t i = t; i < nd; i += BT) {
       double sc = T.dsc2[i];
-      const uint32_t pk = dom_id[i], x = pk & 0xFFFFu;
+      const uint32_t ci = dom_id[i], x = T.tmp[ci];
       if (sc > bs || (sc == bs && x < bi)) {
         bs = sc;
         bi = x;
         bpos = i;
-        bli = pk >> 16;
+        bli = T.cpos[ci];
       }
     }
     double osc;
@@ -1784,6 +1799,7 @@ __device__ Task make_task(const SearchParams &P, Sh &sh, uint32_t *dyn,
   T.list2 = T.list + st;
   T.aux = P.scr.aux + (size_t)cta * st;
   T.tmp = P.scr.tmp + (size_t)cta * 2 * st;
+  T.cpos = P.scr.cpos + (size_t)cta * st;
   T.ssc = P.scr.dsc + (size_t)cta * 3 * st;
   T.cmask = reinterpret_cast<unsigned long long *>(T.ssc + st);
   T.dsc2 = T.ssc + 2 * st;

@@ -258,6 +258,7 @@ static int engine_init(scs_engine *E) {
   // read with 16-byte loads)
   sa.cap_adj = (nnz + 3ull * n + 4 + 3) & ~3ull;
   sa.wit_cap = CL_CAP;
+  sa.max_local = std::min<uint32_t>(n, c.max_local ? c.max_local : MAX_LOCAL_DEFAULT);
   RC(E->dalloc(&sa.loc_off, (size_t)E->nslots * (n + 1), false));
   RC(E->dalloc(&sa.loc_adj, (size_t)E->nslots * sa.cap_adj, false));
   RC(E->dalloc(&sa.loc_dist, (size_t)E->nslots * n, false));
@@ -300,7 +301,7 @@ static int engine_init(scs_engine *E) {
   size_t budget = std::min((size_t)max_optin + (size_t)reserved_i, per_cta);
   budget = budget > (size_t)reserved_i ? budget - (size_t)reserved_i : 0;
   size_t words = budget > stat ? (budget - stat) / 4 : 0;
-  E->nw_smem = (uint32_t)std::min<size_t>(words, std::min<uint32_t>(n, MAX_LOCAL));
+  E->nw_smem = (uint32_t)std::min<size_t>(words, sa.max_local);
   E->smem_bytes = (size_t)E->nw_smem * 4;
   for (const void *k : {(const void *)search_kernel, (const void *)search_kernel_learned}) {
     CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -330,13 +331,14 @@ static int engine_init(scs_engine *E) {
   // per-CTA scratch
   Scratch &sc = E->scr;
   // every per-task index is a local id or a list position, both below
-  // min(n, MAX_LOCAL): size the per-CTA arrays by that, not by n
-  const uint32_t n_loc = std::min<uint32_t>(n, MAX_LOCAL);
+  // the largest local graph: size the per-CTA arrays by that, not by n
+  const uint32_t n_loc = sa.max_local;
   sc.stride = n_loc + 4;
   RC(E->dalloc(&sc.word, (size_t)E->grid * sc.stride));
   RC(E->dalloc(&sc.list, (size_t)E->grid * 2 * sc.stride, false));
   RC(E->dalloc(&sc.aux, (size_t)E->grid * sc.stride));
   RC(E->dalloc(&sc.tmp, (size_t)E->grid * 2 * sc.stride, false));
+  RC(E->dalloc(&sc.cpos, (size_t)E->grid * sc.stride, false));
   RC(E->dalloc(&sc.dsc, (size_t)E->grid * 3 * sc.stride));  // zeroed: scores
   // stacks and pool: the task store is the engine's main memory consumer;
   // stacks get most of what is free (DFS records of the largest local graph),
@@ -610,7 +612,7 @@ static int slice(scs_engine *E) {
       for (uint32_t i = 0; i < cand.size() && rel.size() < need; i++) {
         const uint32_t nl = E->h_slots[cand[i]].n_local;
         const unsigned long long claim =
-            head * (2ull * (nl ? nl : std::min<uint32_t>(E->g.n, MAX_LOCAL)) + 5);
+            head * (2ull * (nl ? nl : E->sa.max_local) + 5);
         if (claim > budget && !(active == 0 && rel.empty())) {
           held = true;
           break;

@@ -41,11 +41,13 @@ prep_kernel(DevGraph g, SlotArrays sa, Slot *slots, const PrepJob *jobs,
 
   const uint32_t nl = build_local_graph(
       g, job.q, job.kl, job.ubd, dist, vis, comp, fa, fb, wpre, lgid, ldist,
-      loff, ladj, sa.cap_adj, min(MAX_LOCAL, sa.stride_n), sh_warp, sh_cnt,
+      loff, ladj, sa.cap_adj, min(sa.max_local, sa.stride_n), sh_warp, sh_cnt,
       &ctr->prep_bytes, &sh_ql);
   if (nl == UINT32_MAX) {
     if (t == 0) {
       sl->status = RS_TOO_LARGE;
+      sl->kl = job.kl;  // the answer is the incumbent
+      sl->kl_heu = job.kl_heu;
       sl->pending = 0;
       __threadfence();
       sl->state = SLOT_DONE;

@@ -165,6 +165,7 @@ static __device__ uint32_t build_local_graph(
       base++;
     }
   }
+  if (t == 0) sh_cnt[2] = 0;
   __syncthreads();
   for (uint32_t i = wid; i < nl; i += PREP_WARPS) {
     uint32_t v = lgid[i];
@@ -174,8 +175,11 @@ static __device__ uint32_t build_local_graph(
     for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
     if (lane == 0) loff[i] = (c + 3u) & ~3u;
     if (lane == 0) fa[i] = c;  // unpadded local degree
+    if (lane == 0 && c > DMASK) atomicOr(&sh_cnt[2], 1u);
   }
   __syncthreads();
+  // the search's state words hold in-task degrees in 15 bits
+  if (sh_cnt[2]) return UINT32_MAX;
   uint32_t total = block_excl_scan(loff, nl, sh_warp);
   if (t == 0) loff[nl] = total;
   __syncthreads();

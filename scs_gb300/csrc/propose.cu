@@ -50,7 +50,7 @@ __device__ void propose_one(const DevGraph &g, const SlotArrays &sa, Slot *slots
   if (*(volatile uint32_t *)&sl->state != SLOT_SEARCH) return;
   const uint32_t n = sl->n_local, q = sl->q_local, l = sl->l, h = sl->h;
   const uint32_t kl0 = *(volatile uint32_t *)&sl->kl;
-  if (n == 0 || n > MAX_LOCAL || h >= CL_CAP || q >= n) return;
+  if (n == 0 || n > sa.max_local || h >= CL_CAP || q >= n) return;
   const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
   const uint32_t *off = sa.loc_off + (size_t)job.slot * (sa.stride_n + 1);
   const uint32_t *adj = sa.loc_adj + (size_t)job.slot * sa.cap_adj;

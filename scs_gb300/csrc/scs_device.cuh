@@ -30,7 +30,11 @@ constexpr uint32_t ST_ABSENT = 0, ST_R = 1, ST_C = 2, ST_X = 3;
 constexpr uint32_t DC_ONE = 1u << 15;
 constexpr uint32_t ST_ONE = 1u << 30;
 constexpr uint32_t DMASK = 0x7FFFu;
-constexpr uint32_t MAX_LOCAL = 32768;  // 15-bit in-task degree fields
+// Largest local graph a query may search unless scs_config.max_local says
+// otherwise (it sizes the per-CTA scratch and the parked roots).  In-task
+// degrees are 15-bit fields of the state word, so a local graph with a
+// vertex of more than DMASK local neighbours is rejected whatever its size.
+constexpr uint32_t MAX_LOCAL_DEFAULT = 1u << 21;
 constexpr uint32_t CL_CAP = 512;       // max |C| tracked (h < CL_CAP)
 constexpr uint32_t MAX_DOMS = 15;      // adjacency mask bits 1..15
 constexpr uint32_t INF16 = 0xFFFFu;
@@ -86,6 +90,7 @@ struct SlotArrays {
   uint64_t cap_adj;
   uint32_t stride_n;
   uint32_t wit_cap;
+  uint32_t max_local;  // largest local graph searched (vertices)
 };
 
 struct Pool {
@@ -135,6 +140,7 @@ struct Scratch {  // per search CTA, stride n words each
   uint32_t *list;  // live ids of the current task (ascending)
   uint32_t *aux;   // marks (zero between uses)
   uint32_t *tmp;   // removal / promotion / candidate lists
+  uint32_t *cpos;  // list positions of the candidates in tmp
   double *dsc;     // candidate scores
   uint32_t stride;
 };

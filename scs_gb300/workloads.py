@@ -165,9 +165,20 @@ def queries_uneven(core, count=10000, seed=QUERY_SEED):
     return np.stack([l, h, q, np.ones(count, int), np.full(count, 10)], 1).astype(np.uint32)
 
 
+def queries_serve(core, count=10000, seed=QUERY_SEED):
+    """Serving: h ~ U[10, 200], l ~ U[3, h/2], q over core >= 12."""
+    rng = np.random.default_rng(seed)
+    cand = np.flatnonzero(core >= 12)
+    q = rng.choice(cand, size=count)
+    h = rng.integers(10, 201, size=count)
+    l = np.array([rng.integers(3, max(3, hh // 2) + 1) for hh in h])
+    return np.stack([l, h, q, np.ones(count, int), np.full(count, 10)], 1).astype(np.uint32)
+
+
 WORKLOADS = {
     # name: (graph builder, query builder)
     "chunglu_n4000": (lambda: chung_lu(4000, 88000, 2.5), queries_small),
     "rmat_s15_ef16": (lambda: rmat(15, 16 << 15), queries_mid),
     "chunglu_n1m": (lambda: chung_lu(1000000, 20000000, 2.3), queries_uneven),
+    "rmat_s22_ef16": (lambda: rmat(22, 16 << 22), queries_serve),
 }

@@ -104,3 +104,26 @@ def test_release_waits_for_pool_room(chunglu_small):
         assert r["degree"] == q["degree"], (q, r)
     assert st["held_memory"] > 0, st
     assert st["releases"] == sum(1 for r in res if r["nodes"] > 0)
+
+
+def test_local_graph_limit_reports_too_large(chunglu_small):
+    """scs_config.max_local bounds the local graph a query may search: with a
+    limit of 64 vertices the 4000-vertex workload's searched queries report
+    SCS_TOO_LARGE (their incumbent as the degree), the others keep their
+    exact answers, and the engine goes on working."""
+    from scs_gb300.engine import DONE, HEURISTIC, TOO_LARGE, Engine
+    g = json.load(open(os.path.join(GOLD, "answers_chunglu_n4000.json")))["queries"]
+    gold = [q for q in g if q["finished"]][:12]
+    rows = [(q["l"], q["h"], q["q"], q["heur"], q["limit_doms"]) for q in gold]
+    eng = Engine(graph=chunglu_small, limit_queries=16, stack_words=1 << 20,
+                 pool_words=1 << 24, max_local=64)
+    try:
+        res = eng.solve(rows)
+    finally:
+        eng.close()
+    assert any(r["status"] == TOO_LARGE for r in res)
+    for q, r in zip(gold, res):
+        if r["status"] == TOO_LARGE:
+            assert r["degree"] == r["kl_heuristic"] <= q["degree"]
+        else:
+            assert r["status"] in (DONE, HEURISTIC) and r["degree"] == q["degree"]
