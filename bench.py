@@ -503,12 +503,20 @@ def main():
     slices = st1["slices"] - st0["slices"]
     peak, peak_kind = measured_peak_gbs()
     achieved = (nbytes / (search_ns / 1e9) / 1e9) if search_ns else 0.0
-    traffic = None
-    tp = os.path.join(ROOT, "profiles", "search_traffic.json")
+    # DRAM bytes per search launch: the DRAM rate an ncu capture measured on
+    # search slices of this same configuration (workload, budget, launch
+    # shape, arm), times this run's mean launch time.  No capture of the
+    # configuration: null.
+    traffic, traffic_src = None, None
+    tp = os.path.join(ROOT, "profiles", "search_traffic_%s.json" % args.workload)
     if os.path.exists(tp) and slices:
         try:
-            rate = float(json.load(open(tp))["dram_bytes_per_ms"])
-            traffic = rate * (search_ns / 1e6) / slices  # DRAM bytes per launch
+            prof = json.load(open(tp))
+            want = {"node_budget": args.node_budget, "ctas_per_sm": tune["ctas_per_sm"],
+                    "active_queries": st1["active"], "slice_us": tune["slice_us"], "arm": arm}
+            if all(prof["config"].get(k) == v for k, v in want.items()):
+                traffic = float(prof["dram_bytes_per_ms"]) * (search_ns / 1e6) / slices
+                traffic_src = os.path.relpath(tp, ROOT)
         except Exception:
             traffic = None
     line = {
@@ -516,13 +524,17 @@ def main():
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * t_dev / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
         "data": "synthetic",
-        "config": {"workload": WORKLOADS[_WL[0]][1], "graph": "R-MAT scale 15, 524288 edges",
+        "config": {"workload": WORKLOADS[_WL[0]][1], "graph": WORKLOADS[_WL[0]][2],
                    "queries": total_q, "exact_answers": exact_all,
                    "all_answers_per_s": total_q / t_dev,
                    "batch": args.batch, "node_budget": args.node_budget,
                    "l2": "flushed between steps (256 MB write)",
                    "exact_fraction": exact / max(len(results), 1),
                    "verified_fraction": verified / max(len(results), 1),
+                   "status_counts": {nm: sum(1 for r in results if r["status"] == st)
+                                     for st, nm in ((0, "done"), (1, "heuristic"), (2, "capacity"),
+                                                    (3, "timeout"), (4, "bad_query"),
+                                                    (5, "too_large"))},
                    "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
                    "nodes": st1["nodes"] - st0["nodes"], "parallelism": "replicas" if world > 1 else "1 GPU",
                    "ctas_per_sm": tune["ctas_per_sm"],
@@ -535,6 +547,7 @@ def main():
                    "compare": compare},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak if peak else None, "traffic": traffic,
+                     "traffic_source": traffic_src,
                      "peak_kind": peak_kind, "kernel": "search_kernel",
                      "launches": slices,
                      "algorithmic_bytes_per_launch": nbytes / max(slices, 1),
