@@ -139,7 +139,7 @@ struct Sh {
 };
 
 __device__ __forceinline__ uint32_t st_of(uint32_t w) { return w >> 30; }
-__device__ __forceinline__ uint32_t dc_of(uint32_t w) { return (w >> 15) & DMASK; }
+__device__ __forceinline__ uint32_t dc_of(uint32_t w) { return (w >> DC_SHIFT) & DCMASK; }
 __device__ __forceinline__ uint32_t dr_of(uint32_t w) { return w & DMASK; }
 __device__ __forceinline__ bool live(uint32_t w) {
   uint32_t s = w >> 30;
@@ -552,7 +552,7 @@ __device__ void load_record(const uint32_t *rec, Task &T, Sh &sh) {
         sh.bad_rec = 1;
         continue;
       }
-      T.W[id] = ((c ? ST_C : ST_R) << 30) | ((dg[j] >> 16) << 15) | (dg[j] & 0xFFFFu);
+      T.W[id] = ((c ? ST_C : ST_R) << 30) | (dg[j] & (ST_ONE - 1u));  // same field layout
       T.list[i] = id;
       if (c) {
         uint32_t k = atomicAdd(&sh.cnt[0], 1u);
@@ -661,6 +661,16 @@ __device__ void rule3(Task &T, Sh &sh) {
     const uint32_t np = sh.cnt[2];
     if (t == 0) sh.r3++;
     if (np == 0) break;
+    if (sh.csize + np > sh.h) {
+      // the task is pruned by size: C only grows here.  The degree updates
+      // are skipped (dC is a 9-bit field, valid while |C| <= h); only the
+      // size reaches the caller.
+      for (uint32_t i = t; i < np; i += BT) T.aux[T.tmp[i]] = 0;
+      __syncthreads();
+      if (t == 0) sh.csize += np;
+      __syncthreads();
+      break;
+    }
     for (uint32_t i = t; i < np; i += BT) {
       uint32_t x = T.tmp[i];
       T.aux[x] = 0;
@@ -1542,7 +1552,7 @@ __device__ __forceinline__ void child_entry(uint32_t x, uint32_t w, uint32_t a,
     inC = inC || is_u || (rk == i + 1);
   }
   ent = (x << 1) | (inC ? 1u : 0u);
-  deg = (dc << 16) | dr;
+  deg = (dc << DC_SHIFT) | dr;
 }
 
 __device__ void mark_children(Task &T, Sh &sh) {
@@ -2394,7 +2404,7 @@ __device__ __forceinline__ void search_body(const SearchParams &P) {
             uint32_t x = T.list[i];
             uint32_t w = T.W[x];
             d[REC_HDR + i] = (x << 1) | (st_of(w) == ST_C ? 1u : 0u);
-            d[REC_HDR + sh.s + i] = (dc_of(w) << 16) | dr_of(w);
+            d[REC_HDR + sh.s + i] = w & (ST_ONE - 1u);  // dC and dR fields
           }
           if (t == 0) {
             d[0] = sh.slot;

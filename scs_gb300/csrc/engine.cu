@@ -1133,7 +1133,7 @@ int scs_debug_step(scs_engine *E, uint32_t ntasks, const uint32_t *task_slot,
         }
       }
       r[REC_HDR + i] = e[i];
-      r[REC_HDR + len + i] = (dc << 16) | dr;
+      r[REC_HDR + len + i] = (dc << DC_SHIFT) | dr;
     }
     for (uint32_t i = 0; i < len; i++) pos[e[i] >> 1] = -1;
     r[0] = s;

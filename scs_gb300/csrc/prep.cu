@@ -97,7 +97,7 @@ prep_kernel(DevGraph g, SlotArrays sa, Slot *slots, const PrepJob *jobs,
     uint32_t dc = (i == ql) ? 0u : ((vis[i >> 5] >> (i & 31)) & 1u);
     uint32_t dr = fa[i] - dc;
     rec[REC_HDR + i] = (i << 1) | (i == ql ? 1u : 0u);
-    rec[REC_HDR + nl + i] = (dc << 16) | dr;
+    rec[REC_HDR + nl + i] = (dc << DC_SHIFT) | dr;
   }
   if (t == 0) {
     if (job.root_to_pool) {

@@ -12,10 +12,12 @@
 // Task record (u32 words):
 //   [0] slot  [1] s  [2] csize  [3] len
 //   [4 .. 4+s)      entries  (local_id << 1) | inC      (ascending id)
-//   [4+s .. 4+2s)   degrees  (dC << 16) | dR            (within the task)
+//   [4+s .. 4+2s)   degrees  (dC << 21) | dR            (within the task)
 //   [4+2s]          footer = len = 2s + 5
 // Per-vertex state word used while a CTA works on a task (shared memory):
-//   bits 31..30 status (0 absent, 1 R, 2 C, 3 removed), 29..15 dC, 14..0 dR.
+//   bits 31..30 status (0 absent, 1 R, 2 C, 3 removed), 29..21 dC, 20..0 dR.
+// dC counts neighbours in C, so dC <= |C| <= h < 512 (9 bits) whenever the
+// task is kept; dR takes the other 21 bits (local degrees up to 2,097,151).
 #pragma once
 #include <cstdint>
 
@@ -27,13 +29,15 @@ namespace scs {
 
 constexpr uint32_t SENT = 0xFFFFFFFFu;
 constexpr uint32_t ST_ABSENT = 0, ST_R = 1, ST_C = 2, ST_X = 3;
-constexpr uint32_t DC_ONE = 1u << 15;
+constexpr uint32_t DC_SHIFT = 21;
+constexpr uint32_t DC_ONE = 1u << DC_SHIFT;
 constexpr uint32_t ST_ONE = 1u << 30;
-constexpr uint32_t DMASK = 0x7FFFu;
+constexpr uint32_t DMASK = DC_ONE - 1u;   // dR field (and the largest dR)
+constexpr uint32_t DCMASK = 0x1FFu;        // dC field after the shift
 // Largest local graph a query may search unless scs_config.max_local says
 // otherwise (it sizes the per-CTA scratch and the parked roots).  In-task
-// degrees are 15-bit fields of the state word, so a local graph with a
-// vertex of more than DMASK local neighbours is rejected whatever its size.
+// dR is a 21-bit field of the state word, so a local graph with a vertex of
+// more than DMASK local neighbours is rejected whatever its size.
 constexpr uint32_t MAX_LOCAL_DEFAULT = 1u << 21;
 constexpr uint32_t CL_CAP = 512;       // max |C| tracked (h < CL_CAP)
 constexpr uint32_t MAX_DOMS = 15;      // adjacency mask bits 1..15

@@ -91,7 +91,8 @@ def _compare_steps(eng, ctxs, tasks):
             assert (s1, c1) == (s2, c2)
             assert np.array_equal(e1, e2)
             dc, dr = ctx.degrees(e2)
-            assert np.array_equal(d2 >> 16, dc) and np.array_equal(d2 & 0xFFFF, dr)
+            # degree words: dC in bits 29..21, dR in bits 20..0
+            assert np.array_equal(d2 >> 21, dc) and np.array_equal(d2 & 0x1FFFFF, dr)
     return got
 
 
