@@ -331,7 +331,14 @@ def run_serve(args):
                            "node_budget": args.node_budget, "slice_us": args.slice_us or 5000,
                            "active_queries": st["active"], "slots": args.slots or 256,
                            "arm": args.arm if args.arm != "auto" else "plain",
-                           "held_by_memory": st["held_memory"]}}
+                           "held_by_memory": st["held_memory"],
+                           "status_counts": {nm: sum(1 for r in res if r["status"] == k)
+                                             for k, nm in ((0, "done"), (1, "heuristic"),
+                                                           (2, "capacity"), (3, "timeout"),
+                                                           (5, "too_large"))},
+                           "engine": {k: st[k] for k in ("nodes", "slices", "prep_ns",
+                                                         "search_ns", "heur_ns",
+                                                         "device_releases")}}}
         print(json.dumps(line), flush=True)
     return 0
 
@@ -355,9 +362,12 @@ def main():
                     help="query slots (0: the batch size, at most 1000)")
     ap.add_argument("--max-local", type=int, default=0,
                     help="largest local graph searched (0: the engine default)")
-    ap.add_argument("--arm", default="auto", choices=["auto", "plain", "learned"],
-                    help="learned: u* and an incumbent proposal from the trained network; "
-                         "plain: the integer rules alone; auto: learned when the model exists")
+    ap.add_argument("--arm", default="plain", choices=["auto", "plain", "learned"],
+                    help="plain (default, the faster arm on this workload): the integer rules "
+                         "alone; learned: u* and an incumbent proposal from the trained "
+                         "network; auto: learned when the model exists")
+    ap.add_argument("--host-release-only", action="store_true",
+                    help="release prepared queries only between slices (no device release)")
     ap.add_argument("--model", default=MODEL, help="model file of the learned arm")
     ap.add_argument("--no-compare", action="store_true",
                     help="skip the other arm's run on the first step's queries")
@@ -415,7 +425,7 @@ def main():
                  node_budget=args.node_budget, stack_words=tune["stack_words"],
                  pool_words=args.pool_words, device=local,
                  active_queries=tune["active_queries"], release_order=args.release_order,
-                 max_local=args.max_local)
+                 max_local=args.max_local, host_release_only=int(args.host_release_only))
     arm = args.arm
     if arm == "auto":  # the model is trained on the mid-size workload
         arm = "learned" if os.path.exists(args.model) and args.workload == "rmat_s15" else "plain"
@@ -544,6 +554,8 @@ def main():
                    "autotune_trials": trials,
                    "arm": arm, "model": os.path.relpath(args.model, ROOT) if arm == "learned" else None,
                    "proposals_better": st1["proposals_better"] - st0["proposals_better"],
+                   "device_releases": st1["device_releases"] - st0["device_releases"],
+                   "host_release_only": bool(args.host_release_only),
                    "compare": compare},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak if peak else None, "traffic": traffic,

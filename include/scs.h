@@ -50,7 +50,7 @@ extern "C" {
                                the reference's Overtime=1 (main.cu:444-463) */
 #define SCS_BAD_QUERY 4     /* malformed query (main.cu:106-109) */
 #define SCS_TOO_LARGE 5     /* filtered graph exceeds the engine's limits
-                               (scs_config.max_local, 15-bit degrees) */
+                               (scs_config.max_local, 21-bit degrees) */
 
 /* Engine configuration.  Field meanings follow the reference CLI where one
  * exists (main.cu:476-502); zero selects the default. */
@@ -88,8 +88,13 @@ typedef struct {
                                  keeps about 13 words of scratch per vertex of
                                  this size, and each slot a parked root of
                                  2*max_local+5 words.  A local graph with a
-                                 vertex of more than 32,767 local neighbours
-                                 is too large at any setting. */
+                                 vertex of more than 2,097,151 local
+                                 neighbours is too large at any setting. */
+  uint32_t host_release_only; /* 1: prepared queries are released only
+                                 between slices; 0 (default): the slice's
+                                 next ones are also queued for the device,
+                                 which releases one each time a searched
+                                 query finishes */
 } scs_config;
 
 /* One query: the reference's message fields (main.cu:92-119). */
@@ -184,7 +189,9 @@ enum {
                              a query's incumbent (model loaded) */
   SCS_STAT_HELD_MEMORY = 20, /* slices in which a prepared query waited for
                              pool room (release_headroom) */
-  SCS_STAT_POOL_FREE = 21  /* shared-pool words free after the last slice */
+  SCS_STAT_POOL_FREE = 21, /* shared-pool words free after the last slice */
+  SCS_STAT_DEVICE_RELEASES = 22 /* prepared queries the device released
+                             inside a slice as searched ones finished */
 };
 int scs_stats(scs_engine *e, uint64_t *out);
 

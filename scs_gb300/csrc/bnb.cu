@@ -1928,12 +1928,42 @@ step_test_kernel(SearchParams P) {
 // ---------------------------------------------------------------------------
 // search: persistent within a time slice
 // ---------------------------------------------------------------------------
+// The next parked root of the slice's release queue goes to the pool (thread
+// 0 of the CTA whose step finished a query).  Its task is counted before its
+// descriptor is visible, and before the finished query's last task leaves
+// the global count, so idle CTAs never see zero outstanding work between the
+// two and leave the slice early.
+__device__ void release_next(const SearchParams &P) {
+  if (!P.rel_count) return;
+  for (;;) {
+    const uint32_t i = atomicAdd(P.rel_next, 1u);
+    if (i >= P.rel_count) return;
+    const uint32_t slot = P.rel_queue[i];
+    Slot *sl = P.slots + slot;
+    if (*(volatile uint32_t *)&sl->state != SLOT_SEARCH) {  // preparation failed
+      P.rel_flag[i] = 2;
+      continue;
+    }
+    sl->t_admit = gtimer();  // search time runs from activation
+    atomicAdd(&P.ctr->pending, 1ull);
+    P.rel_flag[i] = 1;
+    const uint32_t tk = atomicAdd(P.pool.tail, 1u);
+    if (tk >= P.pool.desc_cap) {
+      atomicOr(&P.ctr->error, ERR_POOL);
+      return;
+    }
+    __threadfence();
+    atomicExch(&P.pool.desc[tk], (unsigned long long)slot * P.root_stride + 1ull);
+    return;
+  }
+}
+
 __device__ void finish_tasks(const SearchParams &P, uint32_t slot, long long delta) {
   // delta = tasks created - tasks ended; runs on thread 0.  Only a decrease
   // can finish the query, so only then is the old count waited for.
   Slot *sl = P.slots + slot;
-  atomicAdd(&P.ctr->pending, (unsigned long long)delta);
   if (delta >= 0) {
+    atomicAdd(&P.ctr->pending, (unsigned long long)delta);
     atomicAdd(&sl->pending, (unsigned long long)delta);
     return;
   }
@@ -1943,7 +1973,9 @@ __device__ void finish_tasks(const SearchParams &P, uint32_t slot, long long del
     __threadfence();
     atomicExch(&sl->state, SLOT_DONE);
     atomicAdd(&P.ctr->done_count, 1u);
+    release_next(P);
   }
+  atomicAdd(&P.ctr->pending, (unsigned long long)delta);
 }
 
 // reserve `len` words for a record: own stack, else the shared pool

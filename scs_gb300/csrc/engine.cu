@@ -116,6 +116,9 @@ struct scs_engine {
   std::deque<uint32_t> parked;  // release order (entries of collected slots are skipped)
   uint32_t n_parked = 0;
   uint32_t *d_rel = nullptr;
+  // parked roots queued for release on the device during a slice
+  std::vector<uint32_t> devq;
+  uint32_t *d_relq = nullptr, *d_rel_next = nullptr, *d_rel_flag = nullptr;
   uint32_t active_target = 0;
   unsigned long long pool_free = ~0ull;  // pool words free after the last slice
   Scratch scr{};
@@ -367,6 +370,9 @@ static int engine_init(scs_engine *E) {
   CK(cudaMemcpyAsync(E->pool.arena_top, &E->root_words, 8, cudaMemcpyHostToDevice, E->stream));
   E->pool_free = pw;
   RC(E->dalloc(&E->d_rel, E->nslots, false));
+  RC(E->dalloc(&E->d_relq, E->nslots, false));
+  RC(E->dalloc(&E->d_rel_next, 1));
+  RC(E->dalloc(&E->d_rel_flag, E->nslots));
   // Queries searched at once.  Fewer keep the active local graphs in L2 (the
   // search is bound by dependent loads); enough must stay to feed every CTA
   // through donations.
@@ -588,7 +594,8 @@ static int slice(scs_engine *E) {
     const uint32_t active = E->running - std::min(E->running, E->n_parked);
     const uint32_t need = E->active_target > active ? E->active_target - active : 0;
     std::vector<uint32_t> rel;
-    if (need && E->n_parked) {
+    E->devq.clear();
+    if (E->n_parked && (need || !E->cfg.host_release_only)) {
       // candidates in admission order (entries of collected slots dropped)
       std::vector<uint32_t> cand;
       cand.reserve(E->parked.size());
@@ -609,7 +616,8 @@ static int slice(scs_engine *E) {
       const unsigned long long head = E->cfg.release_headroom ? E->cfg.release_headroom : 4;
       unsigned long long budget = E->pool_free;
       bool held = false;
-      for (uint32_t i = 0; i < cand.size() && rel.size() < need; i++) {
+      uint32_t i = 0;
+      for (; i < cand.size() && rel.size() < need; i++) {
         const uint32_t nl = E->h_slots[cand[i]].n_local;
         const unsigned long long claim =
             head * (2ull * (nl ? nl : E->sa.max_local) + 5);
@@ -621,6 +629,20 @@ static int slice(scs_engine *E) {
         E->slots[cand[i]].parked = false;
         E->n_parked--;
         rel.push_back(cand[i]);
+      }
+      // The next ones, as far as the pool's room goes, are queued for the
+      // device: each time a searched query finishes inside the slice, the
+      // finishing CTA releases the next (release_next in bnb.cu), so the
+      // active set stays full between host round trips.
+      if (!E->cfg.host_release_only && !held) {
+        for (; i < cand.size(); i++) {
+          const uint32_t nl = E->h_slots[cand[i]].n_local;
+          const unsigned long long claim =
+              head * (2ull * (nl ? nl : E->sa.max_local) + 5);
+          if (claim > budget) break;
+          budget -= claim;
+          E->devq.push_back(cand[i]);
+        }
       }
       if (held) E->stats[SCS_STAT_HELD_MEMORY]++;
       std::deque<uint32_t> keep;
@@ -638,8 +660,20 @@ static int slice(scs_engine *E) {
       E->stats[SCS_STAT_RELEASES] += rel.size();
       E->stats[SCS_STAT_H2D] += rel.size() * 4;
     }
+    if (!E->devq.empty()) {
+      CK(cudaMemcpyAsync(E->d_relq, E->devq.data(), E->devq.size() * 4, cudaMemcpyHostToDevice,
+                         E->stream));
+      CK(cudaMemsetAsync(E->d_rel_next, 0, 4, E->stream));
+      CK(cudaMemsetAsync(E->d_rel_flag, 0, E->devq.size() * 4, E->stream));
+      E->stats[SCS_STAT_H2D] += E->devq.size() * 4 + 4;
+    }
   }
   SearchParams P = make_params(E);
+  P.rel_queue = E->d_relq;
+  P.rel_count = (uint32_t)E->devq.size();
+  P.rel_next = E->d_rel_next;
+  P.rel_flag = E->d_rel_flag;
+  P.root_stride = E->root_stride;
   P.slice_ns = t_us * 1000ull;
   // per-slice fields: deadline (set by the first CTA), hungry, error,
   // done_count, stop
@@ -667,10 +701,28 @@ static int slice(scs_engine *E) {
   CK(cudaMemcpyAsync(ph, E->pool.head, 4, cudaMemcpyDeviceToHost, E->stream));
   CK(cudaMemcpyAsync(ph + 1, E->pool.tail, 4, cudaMemcpyDeviceToHost, E->stream));
   CK(cudaMemcpyAsync(&arena_used, E->pool.arena_top, 8, cudaMemcpyDeviceToHost, E->stream));
+  std::vector<uint32_t> rel_flag(E->devq.size());
+  if (!E->devq.empty()) {
+    CK(cudaMemcpyAsync(rel_flag.data(), E->d_rel_flag, rel_flag.size() * 4,
+                       cudaMemcpyDeviceToHost, E->stream));
+    E->stats[SCS_STAT_D2H] += rel_flag.size() * 4;
+  }
   CK(cudaStreamSynchronize(E->stream));
   float ms = 0;
   cudaEventElapsedTime(&ms, E->ev0, E->ev1);
   E->stats[SCS_STAT_SEARCH_NS] += (uint64_t)(ms * 1e6);
+  // roots the device released during the slice are no longer parked (before
+  // collection: such a query may also have finished in this slice)
+  for (size_t i = 0; i < rel_flag.size(); i++) {
+    if (rel_flag[i] != 1) continue;
+    SlotHost &rs = E->slots[E->devq[i]];
+    if (rs.parked) {
+      rs.parked = false;
+      E->n_parked--;
+      E->stats[SCS_STAT_RELEASES]++;
+      E->stats[SCS_STAT_DEVICE_RELEASES]++;
+    }
+  }
   if (E->prep_pending) {
     float pm = 0;
     cudaEventElapsedTime(&pm, E->ev2, E->ev3);

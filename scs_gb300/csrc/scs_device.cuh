@@ -198,6 +198,14 @@ struct SearchParams {
   uint32_t nw_smem;                 // state words that fit in shared memory
   uint32_t nslots;
   unsigned long long slice_ns;      // slice length (device clock)
+  // parked roots the device releases itself, in order, one each time a
+  // searched query finishes inside the slice (the host reads rel_next and
+  // rel_flag after the slice: 1 released, 2 skipped because already done)
+  const uint32_t *rel_queue;
+  uint32_t rel_count;
+  uint32_t *rel_next;
+  uint32_t *rel_flag;
+  unsigned long long root_stride;
   // test mode (one step per CTA)
   const uint32_t *t_rec;            // input records
   const unsigned long long *t_rec_off;

@@ -24,7 +24,8 @@ STATUS_NAMES = {DONE: "done", HEURISTIC: "heuristic", CAPACITY: "capacity",
 STAT_NAMES = ["nodes", "slices", "donations", "steals", "spills", "bytes",
               "prep_bytes", "search_ns", "prep_ns", "launches", "h2d_bytes",
               "d2h_bytes", "heur_ns", "ctas", "smem_words", "errors", "active",
-              "releases", "slides", "proposals_better", "held_memory", "pool_free"]
+              "releases", "slides", "proposals_better", "held_memory", "pool_free",
+              "device_releases"]
 
 
 class Config(C.Structure):
@@ -37,7 +38,7 @@ class Config(C.Structure):
                 ("node_budget", C.c_uint64), ("host_threads", C.c_uint32),
                 ("device", C.c_int32), ("active_queries", C.c_uint32),
                 ("release_order", C.c_uint32), ("release_headroom", C.c_uint32),
-                ("max_local", C.c_uint32)]
+                ("max_local", C.c_uint32), ("host_release_only", C.c_uint32)]
 
 
 class Query(C.Structure):
@@ -307,7 +308,7 @@ class Engine:
     def __init__(self, graph=None, csr=None, limit_queries=64, rules=None,
                  slice_us=0, node_budget=0, ctas_per_sm=0, stack_words=0,
                  pool_words=0, host_threads=0, device=0, active_queries=0,
-                 release_order=0, release_headroom=0, max_local=0):
+                 release_order=0, release_headroom=0, max_local=0, host_release_only=0):
         L = lib()
         cfg = Config()
         cfg.limit_queries = limit_queries
@@ -322,6 +323,7 @@ class Engine:
         cfg.release_order = release_order
         cfg.release_headroom = release_headroom
         cfg.max_local = max_local
+        cfg.host_release_only = host_release_only
         if rules is not None:
             cfg.rules_set = 1
             cfg.red1, cfg.red2, cfg.red3, cfg.prun1, cfg.prun2 = [int(bool(r)) for r in rules]

@@ -293,3 +293,28 @@ def test_engine_matches_reference_gpu_rows(eng_c1):
                 assert r["degree"] == run["degree"], (q, r)
                 answered += 1
     assert answered >= 5
+
+
+def test_device_release_keeps_answers(chunglu_small):
+    """Prepared queries released by the device inside a slice (as searched
+    ones finish) give the same answers as releases between slices only, and
+    every searched query is released exactly once either way."""
+    gold = [g for g in _golden_c1()["queries"] if g["finished"]][:20]
+    rows = [(g["l"], g["h"], g["q"], g["heur"], g["limit_doms"]) for g in gold]
+    out = {}
+    for host_only in (0, 1):
+        e = _engine(graph=chunglu_small, limit_queries=32, active_queries=3,
+                    slice_us=200000, host_release_only=host_only)
+        try:
+            res = e.solve(rows)
+            st = e.stats()
+        finally:
+            e.close()
+        searched = sum(1 for r in res if r["nodes"] > 0)
+        assert st["releases"] == searched, st
+        for g, r in zip(gold, res):
+            assert r["status"] in (0, 1), r
+            assert r["degree"] == g["degree"], (g, r)
+        out[host_only] = st
+    assert out[0]["device_releases"] > 0
+    assert out[1]["device_releases"] == 0
