@@ -152,6 +152,9 @@ struct scs_engine {
 
   int cuda_fail(cudaError_t e, const char *what) {
     err = std::string(what) + ": " + cudaGetErrorString(e);
+    // consume a non-sticky error so that it is not reported again by a later
+    // launch check (of this engine or another one in the process)
+    cudaGetLastError();
     return SCS_ECUDA;
   }
   template <class T>
@@ -596,11 +599,17 @@ static int slice(scs_engine *E) {
     std::vector<uint32_t> rel;
     E->devq.clear();
     if (E->n_parked && (need || !E->cfg.host_release_only)) {
-      // candidates in admission order (entries of collected slots dropped)
+      // candidates in admission order (entries of collected slots dropped).
+      // A slot collected and admitted again before the deque was compacted
+      // has two entries: each slot is taken once.
       std::vector<uint32_t> cand;
+      std::vector<char> seen(E->nslots, 0);
       cand.reserve(E->parked.size());
       for (uint32_t si : E->parked)
-        if (E->slots[si].parked) cand.push_back(si);
+        if (E->slots[si].parked && !seen[si]) {
+          seen[si] = 1;
+          cand.push_back(si);
+        }
       if (E->cfg.release_order == 0 && cand.size() > need) {
         // shortest job first: the smallest local graphs, as read back after
         // the slice that followed their preparation (0 until then, so a
@@ -646,8 +655,12 @@ static int slice(scs_engine *E) {
       }
       if (held) E->stats[SCS_STAT_HELD_MEMORY]++;
       std::deque<uint32_t> keep;
+      std::fill(seen.begin(), seen.end(), 0);
       for (uint32_t si : E->parked)
-        if (E->slots[si].parked) keep.push_back(si);
+        if (E->slots[si].parked && !seen[si]) {
+          seen[si] = 1;
+          keep.push_back(si);
+        }
       E->parked.swap(keep);
     }
     if (!rel.empty()) {
