@@ -523,7 +523,9 @@ def main():
         try:
             prof = json.load(open(tp))
             want = {"node_budget": args.node_budget, "ctas_per_sm": tune["ctas_per_sm"],
-                    "active_queries": st1["active"], "slice_us": tune["slice_us"], "arm": arm}
+                    "active_queries": st1["active"], "slice_us": tune["slice_us"], "arm": arm,
+                    "stack_words": tune["stack_words"], "pool_words": args.pool_words,
+                    "host_release_only": bool(args.host_release_only)}
             if all(prof["config"].get(k) == v for k, v in want.items()):
                 traffic = float(prof["dram_bytes_per_ms"]) * (search_ns / 1e6) / slices
                 traffic_src = os.path.relpath(tp, ROOT)
