@@ -12,6 +12,9 @@ Each file records a checksum of the graph it was computed on, so a change in
 the generators is detected instead of silently comparing different graphs.
 
 Usage: python tests/golden/make_golden.py [heuristic|answers|brute|all]
+       python tests/golden/make_golden.py answers_rmat <count> <node_limit>
+           (answers_rmat_s15_ef16.json: the mid-size workload's first
+           <count> queries; committed with 96 and 30000)
 """
 import hashlib
 import json

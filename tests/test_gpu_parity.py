@@ -112,6 +112,37 @@ def test_step_parity_search_tasks(eng_c1, og_c1, oracle_lib):
     assert 0 in outcomes and len(outcomes) >= 2
 
 
+def test_step_parity_rmat_tasks(rmat15, oracle_lib):
+    """Steps on tasks of the benchmarked mid-size workload (R-MAT scale 15,
+    its first queries with q over core >= 8): header, bounds, u*, dominated
+    vertices, children and witness equal the oracle's, with local graphs of
+    thousands of vertices and hub rows."""
+    from scs_gb300 import workloads as W
+    og = oracle_lib.OracleGraph.from_file(rmat15)
+    cases = []
+    for (l, h, q, hf, ld) in W.queries_mid(og.core, 40).tolist():
+        kl, _ = og.heuristic(0, l, h, q)
+        ku = min(int(og.core[q]), h - 1)
+        if kl < ku:
+            cases.append((l, h, q, ld, kl, int(oracle_lib.lib().orc_ubd_host(kl, h))))
+        if len(cases) == 6:
+            break
+    eng = _engine(graph=rmat15, limit_queries=8)
+    try:
+        qs = [(l, h, q, 0, ld) for (l, h, q, ld, kl, ubd) in cases]
+        eng.debug_prepare(qs, [c[4] for c in cases], [c[5] for c in cases])
+        ctxs, tasks = {}, []
+        for i, (l, h, q, ld, kl, ubd) in enumerate(cases):
+            ctxs[i] = oracle_lib.OracleCtx(og, l, h, q, kl, ubd, ld)
+            for e, k in ctxs[i].collect_tasks(kl, 25):
+                tasks.append((i, k, e))
+        assert len(tasks) >= 100
+        got = _compare_steps(eng, ctxs, tasks)
+    finally:
+        eng.close()
+    assert any(int(g["hdr"][0]) == 0 for g in got)
+
+
 def test_step_parity_random_graphs(oracle_lib):
     """Dense small graphs with rule-3 promotions, dominated vertices and all
     rule subsets."""
@@ -187,6 +218,30 @@ def test_search_chunglu_golden(eng_c1, og_c1):
         c, hq, sz, md = verify_community(og_c1, r["H"], g["q"], g["l"], g["h"])
         if r["h_verified"]:
             assert c and hq and sz and md == r["degree"]
+        if r["status"] == 0 and r["degree"] > g["kl_heu"]:
+            assert r["h_verified"] == 1, r
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(GOLD, "answers_rmat_s15_ef16.json")),
+                    reason="fixture not generated")
+def test_search_rmat_golden(rmat15):
+    """The benchmarked mid-size workload: every query of the fixture that the
+    oracle solves exactly within its node limit gets the same degree from
+    the engine (no task budget), status done or heuristic, and a verified
+    community."""
+    gold_doc = json.load(open(os.path.join(GOLD, "answers_rmat_s15_ef16.json")))
+    gold = [g for g in gold_doc["queries"] if g["finished"]]
+    assert len(gold) >= 8  # of the first 96 queries, 8 finish within 30,000 oracle tasks
+    rows = [(g["l"], g["h"], g["q"], g["heur"], g["limit_doms"]) for g in gold]
+    eng = _engine(graph=rmat15, limit_queries=len(rows))
+    try:
+        res = eng.solve(rows)
+    finally:
+        eng.close()
+    for g, r in zip(gold, res):
+        assert r["status"] in (0, 1), r
+        assert r["kl_heuristic"] == g["kl_heu"]
+        assert r["degree"] == g["degree"], (g, r)
         if r["status"] == 0 and r["degree"] > g["kl_heu"]:
             assert r["h_verified"] == 1, r
 
