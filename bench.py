@@ -515,15 +515,17 @@ def main():
     achieved = (nbytes / (search_ns / 1e9) / 1e9) if search_ns else 0.0
     # DRAM bytes per search launch: the DRAM rate an ncu capture measured on
     # search slices of this same configuration (workload, budget, launch
-    # shape, arm), times this run's mean launch time.  No capture of the
-    # configuration: null.
+    # shape, task store, release mode, arm), times this run's mean launch
+    # time.  No capture of the configuration: null.
     traffic, traffic_src = None, None
     tp = os.path.join(ROOT, "profiles", "search_traffic_%s.json" % args.workload)
     if os.path.exists(tp) and slices:
         try:
             prof = json.load(open(tp))
+            # the slice length only scales the launch; the DRAM rate per ms is
+            # what the capture measured, so it is not matched
             want = {"node_budget": args.node_budget, "ctas_per_sm": tune["ctas_per_sm"],
-                    "active_queries": st1["active"], "slice_us": tune["slice_us"], "arm": arm,
+                    "active_queries": st1["active"], "arm": arm,
                     "stack_words": tune["stack_words"], "pool_words": args.pool_words,
                     "host_release_only": bool(args.host_release_only)}
             if all(prof["config"].get(k) == v for k, v in want.items()):
