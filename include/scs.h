@@ -397,7 +397,26 @@ int scs_debug_step(scs_engine *e, uint32_t ntasks, const uint32_t *task_slot,
                    const uint32_t *task_len, const uint32_t *task_entries,
                    uint32_t *out_hdr, uint32_t *out_doms, uint32_t doms_stride,
                    uint32_t *out_kids, uint64_t kids_stride, uint32_t *out_wit,
-                   uint32_t wit_stride);
+                   uint32_t wit_stride, const uint32_t *force, uint32_t *out_sl,
+                   float *out_sl_feat);
+/* (scs_debug_step, continued) force (may be NULL): per task the local id
+ * of u* to branch on instead of the rule's choice (a candidate: an R vertex
+ * with a C neighbour; 0xFFFFFFFF keeps the rule's).  out_sl / out_sl_feat
+ * (both or neither): per task the learned-branching shortlist, [count, 16
+ * local ids] and 16 x 16 features. */
+
+/* Strong-branching lookahead for training the branching network (no
+ * reference counterpart): for each task, one step that branches on
+ * force[t], then one step on each of its children.  out_hdr gets the forced
+ * step's header (16 per task), out_nkids its children, out_branching how
+ * many of them still branch after their own reductions and bounds, and
+ * out_cost the sum of those children's live sizes (the work left below this
+ * choice of u*, one level down). */
+int scs_debug_lookahead(scs_engine *e, uint32_t ntasks, const uint32_t *task_slot,
+                        const uint32_t *kl_in, const uint64_t *task_off,
+                        const uint32_t *task_len, const uint32_t *task_entries,
+                        const uint32_t *force, uint32_t *out_hdr, uint32_t *out_nkids,
+                        uint32_t *out_branching, uint64_t *out_cost);
 
 #ifdef __cplusplus
 }

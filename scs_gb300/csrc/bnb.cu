@@ -1181,7 +1181,9 @@ __device__ void learned_choice(const SearchParams &P, Task &T, Sh &sh) {
     __syncwarp();
     const bool score = (sh.lrn & 1u) && nsl >= 2;
     const bool trace = (sh.lrn & 2u) && nsl >= 1;
-    if (score || trace) {
+    const bool tout = (sh.lrn & 4u) != 0;  // one-step test: shortlist out
+    if (tout && lane == 0) P.t_sl[(size_t)blockIdx.x * (MLP_TILE + 1)] = nsl;
+    if (score || trace || tout) {
       FeatTask k;
       k.s = sh.csize + sh.nR;
       k.csize = sh.csize;
@@ -1236,6 +1238,13 @@ __device__ void learned_choice(const SearchParams &P, Task &T, Sh &sh) {
           sh.ustar = bi;
           sh.us_idx = bp;
         }
+      }
+      if (tout && (uint32_t)lane < nsl) {
+        P.t_sl[(size_t)blockIdx.x * (MLP_TILE + 1) + 1 + lane] = sh.sl_id[lane];
+        const float *f = sh.feat + lane * (MLP_IN + 1);
+        float *dst = P.t_sl_feat + ((size_t)blockIdx.x * MLP_TILE + lane) * MLP_IN;
+#pragma unroll
+        for (int j = 0; j < MLP_IN; j++) dst[j] = f[j];
       }
       if (trace) {
         unsigned long long base = 0;
@@ -1776,6 +1785,26 @@ __device__ void step_core(const SearchParams &P, Task &T, Sh &sh, bool test,
     return;
   }
   choose_ustar<LRN>(P, T, sh);
+  if (test && P.t_force) {
+    // one-step test: branch on the given vertex instead of the rule's u*
+    // (the caller passes a candidate: an R vertex with a C neighbour)
+    if (t == 0) {
+      const uint32_t f = P.t_force[blockIdx.x];
+      if (f != SENT && sh.ustar != UINT32_MAX) {
+        uint32_t lo = 0, hi = sh.s;  // T.list ascends over the live entries
+        while (lo < hi) {
+          const uint32_t mid = (lo + hi) >> 1;
+          if (T.list[mid] < f) lo = mid + 1;
+          else hi = mid;
+        }
+        if (lo < sh.s && T.list[lo] == f) {
+          sh.ustar = f;
+          sh.us_idx = lo;
+        }
+      }
+    }
+    __syncthreads();
+  }
   phase_mark(sh, 4);
   if (sh.ustar == UINT32_MAX) {
     clear_scores(T, sh);
@@ -1876,13 +1905,14 @@ step_test_kernel(SearchParams P) {
   Task T = make_task(P, sh, dyn, ti);
   // state words and the bitmap behind them start at zero
   for (uint32_t i = threadIdx.x; i < P.nw_smem; i += BT) dyn[i] = 0;
+  if (threadIdx.x == 0) sh.lrn = P.t_sl ? 4u : 0u;
   __syncthreads();
   load_record(rec, T, sh);
   uint32_t *wit = P.t_wit + (size_t)ti * P.t_wit_stride;
-  step_core<false>(P, T, sh, true, wit);
+  step_core<true>(P, T, sh, true, wit);
   uint32_t *hdr = P.t_hdr + 16 * ti;
-  uint32_t *kids = P.t_kids + (size_t)ti * P.t_kids_stride;
-  if (sh.outcome == 0) {
+  uint32_t *kids = P.t_kids ? P.t_kids + (size_t)ti * P.t_kids_stride : nullptr;
+  if (sh.outcome == 0 && kids) {
     const uint32_t k = sh.ndoms;
     uint64_t w = 0;
     uint32_t nk = 0;
@@ -1890,16 +1920,26 @@ step_test_kernel(SearchParams P) {
       uint32_t s2, c2;
       child_shape(sh, code, s2, c2);
       if (!child_alive(sh, s2, c2)) continue;
-      // layout for the test: [s, csize, entries(s), degrees(s)]
       uint32_t *dst = kids + w;
-      write_child(T, sh, code, dst + 2, dst + 2 + s2, nullptr);
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        dst[0] = s2;
-        dst[1] = c2;
+      if (P.t_kids_rec) {
+        // full task records, as the search stores them
+        write_child(T, sh, code, dst + REC_HDR, dst + REC_HDR + s2, dst);
+        __syncthreads();
+        if (threadIdx.x == 0 && nk < MAX_DOMS + 2)
+          P.t_kid_off[(size_t)ti * (MAX_DOMS + 3) + nk] = (uint32_t)w;
+        __syncthreads();
+        w += 2ull * s2 + 5;
+      } else {
+        // layout for the parity tests: [s, csize, entries(s), degrees(s)]
+        write_child(T, sh, code, dst + 2, dst + 2 + s2, nullptr);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          dst[0] = s2;
+          dst[1] = c2;
+        }
+        __syncthreads();
+        w += 2 + 2ull * s2;
       }
-      __syncthreads();
-      w += 2 + 2ull * s2;
       nk++;
     }
     if (threadIdx.x == 0) {
@@ -1919,6 +1959,7 @@ step_test_kernel(SearchParams P) {
     hdr[7] = sh.ustar;
     hdr[8] = sh.ndoms;
     hdr[11] = wit[CL_CAP];
+    if (sh.outcome == 0 && !kids) hdr[9] = 0;
     for (uint32_t j = 0; j < sh.ndoms; j++)
       P.t_doms[(size_t)ti * P.t_doms_stride + j] = sh.doms[j];
   }

@@ -1148,16 +1148,15 @@ int scs_debug_local_graph(scs_engine *E, uint32_t slot, uint32_t *gid,
 // One deterministic step per task on prepared slots.  Task entries are
 // (local_id<<1)|inC, ascending; the input degrees are computed here from the
 // slot's local graph.
-int scs_debug_step(scs_engine *E, uint32_t ntasks, const uint32_t *task_slot,
-                   const uint32_t *kl_in, const uint64_t *task_off,
-                   const uint32_t *task_len, const uint32_t *task_entries,
-                   uint32_t *out_hdr, uint32_t *out_doms, uint32_t doms_stride,
-                   uint32_t *out_kids, uint64_t kids_stride, uint32_t *out_wit,
-                   uint32_t wit_stride) {
-  if (!E || !ntasks) return SCS_EINVAL;
-  if (wit_stride < CL_CAP + 1 || doms_stride < MAX_DOMS) return SCS_EINVAL;
+}  // extern "C"
+
+// Task records (with in-task degrees recounted on the host) for the given
+// tasks of prepared slots, for the one-step test kernel.
+static int build_test_records(scs_engine *E, uint32_t ntasks, const uint32_t *task_slot,
+                              const uint64_t *task_off, const uint32_t *task_len,
+                              const uint32_t *task_entries, std::vector<uint32_t> &recs,
+                              std::vector<unsigned long long> &roff) {
   const uint32_t n = E->g.n;
-  // local graphs of the slots used
   std::vector<std::vector<uint32_t>> loff(E->nslots), ladj(E->nslots);
   for (uint32_t t = 0; t < ntasks; t++) {
     uint32_t s = task_slot[t];
@@ -1165,8 +1164,7 @@ int scs_debug_step(scs_engine *E, uint32_t ntasks, const uint32_t *task_slot,
     if (!loff[s].empty()) continue;
     CK(cudaMemcpy(&E->h_slots[s], E->d_slots + s, sizeof(Slot), cudaMemcpyDeviceToHost));
     uint32_t nl = E->h_slots[s].n_local;
-    loff[s].resize(nl + 1);
-    std::vector<uint32_t> o(nl + 1), a(n + 1);
+    std::vector<uint32_t> o(nl + 1);
     int rc = scs_debug_local_graph(E, s, nullptr, o.data(), nullptr, nullptr);
     if (rc) return rc;
     std::vector<uint32_t> aa(o[nl] + 1);
@@ -1175,9 +1173,8 @@ int scs_debug_step(scs_engine *E, uint32_t ntasks, const uint32_t *task_slot,
     loff[s] = o;
     ladj[s] = aa;
   }
-  // records with degrees
-  std::vector<uint32_t> recs;
-  std::vector<unsigned long long> roff(ntasks);
+  recs.clear();
+  roff.assign(ntasks, 0);
   std::vector<int32_t> pos(n, -1);
   for (uint32_t t = 0; t < ntasks; t++) {
     uint32_t s = task_slot[t], len = task_len[t];
@@ -1191,9 +1188,9 @@ int scs_debug_step(scs_engine *E, uint32_t ntasks, const uint32_t *task_slot,
       uint32_t v = e[i] >> 1, dc = 0, dr = 0;
       cs += e[i] & 1u;
       for (uint32_t k = loff[s][v]; k < loff[s][v + 1]; k++) {
-        int32_t j = pos[ladj[s][k]];
-        if (j >= 0) {
-          if (e[j] & 1u) dc++;
+        int32_t jj = pos[ladj[s][k]];
+        if (jj >= 0) {
+          if (e[jj] & 1u) dc++;
           else dr++;
         }
       }
@@ -1207,34 +1204,63 @@ int scs_debug_step(scs_engine *E, uint32_t ntasks, const uint32_t *task_slot,
     r[3] = 2 * len + 5;
     r[REC_HDR + 2 * len] = 2 * len + 5;
   }
-  uint32_t *d_rec = nullptr, *d_hdr = nullptr, *d_doms = nullptr, *d_kids = nullptr,
-           *d_wit = nullptr, *d_kl = nullptr;
-  unsigned long long *d_roff = nullptr;
-  int rc = 0;
-  auto cleanup = [&]() {
-    cudaFree(d_rec); cudaFree(d_hdr); cudaFree(d_doms); cudaFree(d_kids);
-    cudaFree(d_wit); cudaFree(d_kl); cudaFree(d_roff);
-  };
-  const uint32_t chunk = E->grid;
-  for (uint32_t base = 0; base < ntasks && !rc; base += chunk) {
-    uint32_t cnt = std::min(chunk, ntasks - base);
-    if (!d_rec) {
-      if (cudaMalloc(&d_rec, recs.size() * 4) || cudaMalloc(&d_roff, ntasks * 8ull) ||
-          cudaMalloc(&d_hdr, 16ull * chunk * 4) ||
-          cudaMalloc(&d_doms, (size_t)doms_stride * chunk * 4) ||
-          cudaMalloc(&d_kids, kids_stride * chunk * 4) ||
-          cudaMalloc(&d_wit, (size_t)wit_stride * chunk * 4) ||
-          cudaMalloc(&d_kl, ntasks * 4ull)) {
-        cleanup();
-        E->err = "debug step allocation failed";
-        return SCS_ENOMEM;
-      }
-      cudaMemcpy(d_rec, recs.data(), recs.size() * 4, cudaMemcpyHostToDevice);
-      cudaMemcpy(d_roff, roff.data(), ntasks * 8ull, cudaMemcpyHostToDevice);
-      cudaMemcpy(d_kl, kl_in, ntasks * 4ull, cudaMemcpyHostToDevice);
+  return 0;
+}
+
+// Device buffers of a one-step test run (freed on destruction).
+struct TestBufs {
+  std::vector<void *> p;
+  template <class T>
+  bool get(T **ptr, size_t count) {
+    if (cudaMalloc((void **)ptr, std::max<size_t>(count, 1) * sizeof(T)) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
     }
-    cudaMemset(d_hdr, 0, 16ull * chunk * 4);
-    cudaMemset(d_wit, 0, (size_t)wit_stride * chunk * 4);
+    p.push_back(*ptr);
+    return true;
+  }
+  ~TestBufs() {
+    for (void *q : p) cudaFree(q);
+  }
+};
+
+extern "C" {
+
+int scs_debug_step(scs_engine *E, uint32_t ntasks, const uint32_t *task_slot,
+                   const uint32_t *kl_in, const uint64_t *task_off,
+                   const uint32_t *task_len, const uint32_t *task_entries,
+                   uint32_t *out_hdr, uint32_t *out_doms, uint32_t doms_stride,
+                   uint32_t *out_kids, uint64_t kids_stride, uint32_t *out_wit,
+                   uint32_t wit_stride, const uint32_t *force, uint32_t *out_sl,
+                   float *out_sl_feat) {
+  if (!E || !ntasks) return SCS_EINVAL;
+  if (wit_stride < CL_CAP + 1 || doms_stride < MAX_DOMS) return SCS_EINVAL;
+  std::vector<uint32_t> recs;
+  std::vector<unsigned long long> roff;
+  RC(build_test_records(E, ntasks, task_slot, task_off, task_len, task_entries, recs, roff));
+  const uint32_t chunk = E->grid;
+  TestBufs B;
+  uint32_t *d_rec, *d_hdr, *d_doms, *d_kids, *d_wit, *d_kl, *d_force = nullptr, *d_sl = nullptr;
+  float *d_slf = nullptr;
+  unsigned long long *d_roff;
+  if (!B.get(&d_rec, recs.size()) || !B.get(&d_roff, ntasks) || !B.get(&d_hdr, 16ull * chunk) ||
+      !B.get(&d_doms, (size_t)doms_stride * chunk) || !B.get(&d_kids, kids_stride * chunk) ||
+      !B.get(&d_wit, (size_t)wit_stride * chunk) || !B.get(&d_kl, ntasks) ||
+      (force && !B.get(&d_force, ntasks)) ||
+      (out_sl && !B.get(&d_sl, (size_t)(MLP_TILE + 1) * chunk)) ||
+      (out_sl_feat && !B.get(&d_slf, (size_t)MLP_TILE * MLP_IN * chunk))) {
+    E->err = "debug step allocation failed";
+    return SCS_ENOMEM;
+  }
+  CK(cudaMemcpy(d_rec, recs.data(), recs.size() * 4, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d_roff, roff.data(), ntasks * 8ull, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d_kl, kl_in, ntasks * 4ull, cudaMemcpyHostToDevice));
+  if (force) CK(cudaMemcpy(d_force, force, ntasks * 4ull, cudaMemcpyHostToDevice));
+  for (uint32_t base = 0; base < ntasks; base += chunk) {
+    uint32_t cnt = std::min(chunk, ntasks - base);
+    CK(cudaMemset(d_hdr, 0, 16ull * chunk * 4));
+    CK(cudaMemset(d_wit, 0, (size_t)wit_stride * chunk * 4));
+    if (d_sl) CK(cudaMemset(d_sl, 0, (size_t)(MLP_TILE + 1) * chunk * 4));
     SearchParams P = make_params(E);
     P.t_rec = d_rec;
     P.t_rec_off = d_roff + base;
@@ -1247,25 +1273,148 @@ int scs_debug_step(scs_engine *E, uint32_t ntasks, const uint32_t *task_slot,
     P.t_wit = d_wit;
     P.t_wit_stride = wit_stride;
     P.t_kl = d_kl + base;
-    cudaFuncSetAttribute(step_test_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)E->smem_bytes);
-    step_test_kernel<<<cnt, SEARCH_THREADS, E->smem_bytes, E->stream>>>(P);
-    cudaError_t e = cudaStreamSynchronize(E->stream);
-    if (e == cudaSuccess) e = cudaGetLastError();
-    if (e != cudaSuccess) {
-      cleanup();
-      return E->cuda_fail(e, "step_test_kernel");
+    P.t_force = d_force ? d_force + base : nullptr;
+    P.t_sl = d_sl;
+    P.t_sl_feat = d_slf;
+    if (d_sl && !d_slf) {
+      E->err = "the shortlist needs its feature buffer";
+      return SCS_EINVAL;
     }
-    cudaMemcpy(out_hdr + 16ull * base, d_hdr, 16ull * cnt * 4, cudaMemcpyDeviceToHost);
-    cudaMemcpy(out_doms + (size_t)doms_stride * base, d_doms, (size_t)doms_stride * cnt * 4,
-               cudaMemcpyDeviceToHost);
-    cudaMemcpy(out_kids + kids_stride * base, d_kids, kids_stride * cnt * 4,
-               cudaMemcpyDeviceToHost);
-    cudaMemcpy(out_wit + (size_t)wit_stride * base, d_wit, (size_t)wit_stride * cnt * 4,
-               cudaMemcpyDeviceToHost);
+    CK(cudaFuncSetAttribute(step_test_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)E->smem_bytes));
+    step_test_kernel<<<cnt, SEARCH_THREADS, E->smem_bytes, E->stream>>>(P);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(E->stream));
+    CK(cudaMemcpy(out_hdr + 16ull * base, d_hdr, 16ull * cnt * 4, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(out_doms + (size_t)doms_stride * base, d_doms, (size_t)doms_stride * cnt * 4,
+                  cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(out_kids + kids_stride * base, d_kids, kids_stride * cnt * 4,
+                  cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(out_wit + (size_t)wit_stride * base, d_wit, (size_t)wit_stride * cnt * 4,
+                  cudaMemcpyDeviceToHost));
+    if (out_sl)
+      CK(cudaMemcpy(out_sl + (size_t)(MLP_TILE + 1) * base, d_sl,
+                    (size_t)(MLP_TILE + 1) * cnt * 4, cudaMemcpyDeviceToHost));
+    if (out_sl_feat)
+      CK(cudaMemcpy(out_sl_feat + (size_t)MLP_TILE * MLP_IN * base, d_slf,
+                    (size_t)MLP_TILE * MLP_IN * cnt * 4, cudaMemcpyDeviceToHost));
   }
-  cleanup();
-  return rc;
+  return 0;
+}
+
+int scs_debug_lookahead(scs_engine *E, uint32_t ntasks, const uint32_t *task_slot,
+                        const uint32_t *kl_in, const uint64_t *task_off,
+                        const uint32_t *task_len, const uint32_t *task_entries,
+                        const uint32_t *force, uint32_t *out_hdr, uint32_t *out_nkids,
+                        uint32_t *out_branching, uint64_t *out_cost) {
+  if (!E || !ntasks || !force || !out_hdr || !out_nkids || !out_branching || !out_cost)
+    return SCS_EINVAL;
+  std::vector<uint32_t> recs;
+  std::vector<unsigned long long> roff;
+  RC(build_test_records(E, ntasks, task_slot, task_off, task_len, task_entries, recs, roff));
+  uint32_t maxlen = 1;
+  for (uint32_t t = 0; t < ntasks; t++) maxlen = std::max(maxlen, task_len[t]);
+  const uint64_t kstride = (uint64_t)(MAX_DOMS + 2) * (2ull * maxlen + 5);
+  const uint32_t chunk = std::min<uint32_t>(E->grid, 128);
+  const uint32_t koff_stride = MAX_DOMS + 3;
+  TestBufs B;
+  uint32_t *d_rec, *d_hdr, *d_doms, *d_kids, *d_wit, *d_kl, *d_force, *d_koff, *d_ckl,
+      *d_chdr;
+  unsigned long long *d_roff, *d_croff;
+  const uint32_t cmax = chunk * (MAX_DOMS + 2);
+  if (!B.get(&d_rec, recs.size()) || !B.get(&d_roff, ntasks) || !B.get(&d_hdr, 16ull * chunk) ||
+      !B.get(&d_doms, (size_t)MAX_DOMS * cmax) || !B.get(&d_kids, kstride * chunk) ||
+      !B.get(&d_wit, (size_t)(CL_CAP + 1) * cmax) || !B.get(&d_kl, ntasks) ||
+      !B.get(&d_force, ntasks) || !B.get(&d_koff, (size_t)koff_stride * chunk) ||
+      !B.get(&d_ckl, cmax) || !B.get(&d_chdr, 16ull * cmax) || !B.get(&d_croff, cmax)) {
+    E->err = "lookahead allocation failed";
+    return SCS_ENOMEM;
+  }
+  CK(cudaMemcpy(d_rec, recs.data(), recs.size() * 4, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d_roff, roff.data(), ntasks * 8ull, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d_kl, kl_in, ntasks * 4ull, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d_force, force, ntasks * 4ull, cudaMemcpyHostToDevice));
+  CK(cudaFuncSetAttribute(step_test_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                          (int)E->smem_bytes));
+  std::vector<uint32_t> hdr(16ull * chunk), koff((size_t)koff_stride * chunk);
+  std::vector<unsigned long long> croff;
+  std::vector<uint32_t> ckl, cparent, chdr;
+  for (uint32_t base = 0; base < ntasks; base += chunk) {
+    const uint32_t cnt = std::min(chunk, ntasks - base);
+    CK(cudaMemset(d_hdr, 0, 16ull * chunk * 4));
+    CK(cudaMemset(d_wit, 0, (size_t)(CL_CAP + 1) * chunk * 4));
+    // 1. the forced step of each task, children written as task records
+    SearchParams P = make_params(E);
+    P.t_rec = d_rec;
+    P.t_rec_off = d_roff + base;
+    P.t_ntasks = cnt;
+    P.t_hdr = d_hdr;
+    P.t_doms = d_doms;
+    P.t_doms_stride = MAX_DOMS;
+    P.t_kids = d_kids;
+    P.t_kids_stride = kstride;
+    P.t_wit = d_wit;
+    P.t_wit_stride = CL_CAP + 1;
+    P.t_kl = d_kl + base;
+    P.t_force = d_force + base;
+    P.t_kids_rec = 1;
+    P.t_kid_off = d_koff;
+    step_test_kernel<<<cnt, SEARCH_THREADS, E->smem_bytes, E->stream>>>(P);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(E->stream));
+    CK(cudaMemcpy(hdr.data(), d_hdr, 16ull * cnt * 4, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(koff.data(), d_koff, (size_t)koff_stride * cnt * 4, cudaMemcpyDeviceToHost));
+    croff.clear();
+    ckl.clear();
+    cparent.clear();
+    for (uint32_t i = 0; i < cnt; i++) {
+      const uint32_t *h = hdr.data() + 16 * i;
+      std::copy(h, h + 16, out_hdr + 16ull * (base + i));
+      out_nkids[base + i] = h[0] == 0 ? h[9] : 0;
+      out_branching[base + i] = 0;
+      out_cost[base + i] = 0;
+      if (h[0] != 0) continue;
+      for (uint32_t j = 0; j < h[9] && j < MAX_DOMS + 2; j++) {
+        croff.push_back((unsigned long long)i * kstride + koff[(size_t)koff_stride * i + j]);
+        ckl.push_back(h[1]);  // the incumbent after the parent's step
+        cparent.push_back(base + i);
+      }
+    }
+    if (croff.empty()) continue;
+    // 2. one step on every child (no children of theirs written)
+    const uint32_t nc = (uint32_t)croff.size();
+    CK(cudaMemcpy(d_croff, croff.data(), nc * 8ull, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(d_ckl, ckl.data(), nc * 4ull, cudaMemcpyHostToDevice));
+    CK(cudaMemset(d_chdr, 0, 16ull * nc * 4));
+    CK(cudaMemset(d_wit, 0, (size_t)(CL_CAP + 1) * std::min(nc, cmax) * 4));
+    for (uint32_t cb = 0; cb < nc; cb += E->grid) {
+      const uint32_t cc = std::min<uint32_t>(E->grid, nc - cb);
+      SearchParams Q = make_params(E);
+      Q.t_rec = d_kids;
+      Q.t_rec_off = d_croff + cb;
+      Q.t_ntasks = cc;
+      Q.t_hdr = d_chdr + 16ull * cb;
+      Q.t_doms = d_doms;
+      Q.t_doms_stride = MAX_DOMS;
+      Q.t_kids = nullptr;
+      Q.t_wit = d_wit;
+      Q.t_wit_stride = CL_CAP + 1;
+      Q.t_kl = d_ckl + cb;
+      step_test_kernel<<<cc, SEARCH_THREADS, E->smem_bytes, E->stream>>>(Q);
+      CK(cudaGetLastError());
+      CK(cudaStreamSynchronize(E->stream));
+    }
+    chdr.resize(16ull * nc);
+    CK(cudaMemcpy(chdr.data(), d_chdr, 16ull * nc * 4, cudaMemcpyDeviceToHost));
+    // 3. cost: the live size of every child that still branches
+    for (uint32_t c = 0; c < nc; c++) {
+      const uint32_t *h = chdr.data() + 16ull * c;
+      if (h[0] != 0) continue;
+      out_branching[cparent[c]]++;
+      out_cost[cparent[c]] += h[4];
+    }
+  }
+  return 0;
 }
 
 }  // extern "C"

@@ -218,6 +218,14 @@ struct SearchParams {
   uint32_t *t_wit;
   uint32_t t_wit_stride;
   const uint32_t *t_kl;             // incumbent per test task
+  const uint32_t *t_force;          // u* forced per test task (local id;
+                                    // SENT: the rule's own), or null
+  uint32_t *t_sl;                   // per test task: [count, 16 local ids] of
+                                    // the shortlist, or null
+  float *t_sl_feat;                 // per test task: 16 x 16 features
+  uint32_t t_kids_rec;              // 1: children written as full task
+                                    // records, their offsets in t_kid_off
+  uint32_t *t_kid_off;              // per test task: 18 child offsets
   // learned branching: packed network (w == null: the plain method) and the
   // trace the exact solver emits for training (cap == 0: none)
   MlpDev mlp;

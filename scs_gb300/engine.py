@@ -180,7 +180,9 @@ def lib(build_if_missing=False):
     L.scs_debug_local_graph.argtypes = [vp, C.c_uint32, _u32p, _u32p, _u32p, _u32p]
     L.scs_debug_step.argtypes = [vp, C.c_uint32, _u32p, _u32p, _u64p, _u32p, _u32p,
                                  _u32p, _u32p, C.c_uint32, _u32p, C.c_uint64, _u32p,
-                                 C.c_uint32]
+                                 C.c_uint32, _u32p, _u32p, C.POINTER(C.c_float)]
+    L.scs_debug_lookahead.argtypes = [vp, C.c_uint32, _u32p, _u32p, _u64p, _u32p, _u32p,
+                                      _u32p, _u32p, _u32p, _u32p, _u64p]
     fp = C.POINTER(C.c_float)
     L.scs_load_model.argtypes = [vp, C.c_char_p]
     L.scs_trace_enable.argtypes = [vp, C.c_uint64, C.c_uint32]
@@ -452,9 +454,40 @@ class Engine:
                     "scs_debug_local_graph")
         return gid[:n_local], off, adj[: off[-1]], dist[:n_local]
 
-    def debug_step(self, tasks, kids_stride=None):
+    @staticmethod
+    def _task_arrays(tasks):
+        nt = len(tasks)
+        slots = np.array([t[0] for t in tasks], dtype=np.uint32)
+        kls = np.array([t[1] for t in tasks], dtype=np.uint32)
+        lens = np.array([len(t[2]) for t in tasks], dtype=np.uint32)
+        offs = np.zeros(nt, dtype=np.uint64)
+        offs[1:] = np.cumsum(lens[:-1].astype(np.uint64))
+        ent = (np.concatenate([np.asarray(t[2], dtype=np.uint32) for t in tasks])
+               if nt else np.zeros(1, np.uint32))
+        return nt, slots, kls, lens, offs, ent
+
+    def debug_lookahead(self, tasks, force):
+        """Strong-branching lookahead: for each task (slot, kl, entries) the
+        step that branches on force[i] (a local id), then one step on each
+        child.  Returns (hdr[n][16], nkids, branching, cost)."""
+        nt, slots, kls, lens, offs, ent = self._task_arrays(tasks)
+        f = np.ascontiguousarray(force, dtype=np.uint32)
+        hdr = np.zeros(16 * nt, dtype=np.uint32)
+        nk = np.zeros(nt, dtype=np.uint32)
+        br = np.zeros(nt, dtype=np.uint32)
+        cost = np.zeros(nt, dtype=np.uint64)
+        self._check(lib().scs_debug_lookahead(self._h, nt, _p(slots), _p(kls),
+                                              offs.ctypes.data_as(_u64p), _p(lens), _p(ent),
+                                              _p(f), _p(hdr), _p(nk), _p(br),
+                                              cost.ctypes.data_as(_u64p)),
+                    "scs_debug_lookahead")
+        return hdr.reshape(nt, 16), nk, br, cost
+
+    def debug_step(self, tasks, kids_stride=None, force=None, shortlist=False):
         """tasks: list of (slot, kl, entries[uint32 (id<<1)|inC]).  Returns a
-        list of dicts with hdr, doms, kids, wit."""
+        list of dicts with hdr, doms, kids, wit (and sl_ids, sl_feat with
+        shortlist=True).  force: per task a local id to branch on, or
+        0xFFFFFFFF for the rule's u*."""
         nt = len(tasks)
         slots = np.array([t[0] for t in tasks], dtype=np.uint32)
         kls = np.array([t[1] for t in tasks], dtype=np.uint32)
@@ -468,9 +501,15 @@ class Engine:
         doms = np.zeros(16 * nt, dtype=np.uint32)
         kids = np.zeros(ks * nt, dtype=np.uint32)
         wit = np.zeros(513 * nt, dtype=np.uint32)
+        fa = None if force is None else np.ascontiguousarray(force, dtype=np.uint32)
+        sl = np.zeros(17 * nt, dtype=np.uint32) if shortlist else None
+        slf = np.zeros(16 * 16 * nt, dtype=np.float32) if shortlist else None
         self._check(lib().scs_debug_step(self._h, nt, _p(slots), _p(kls),
                                          offs.ctypes.data_as(_u64p), _p(lens), _p(ent),
-                                         _p(hdr), _p(doms), 16, _p(kids), ks, _p(wit), 513),
+                                         _p(hdr), _p(doms), 16, _p(kids), ks, _p(wit), 513,
+                                         None if fa is None else _p(fa),
+                                         None if sl is None else _p(sl),
+                                         None if slf is None else _fp(slf)),
                     "scs_debug_step")
         out = []
         for i in range(nt):
@@ -483,8 +522,13 @@ class Engine:
                 children.append((s2, c2, k[w + 2: w + 2 + s2].copy(), k[w + 2 + s2: w + 2 + 2 * s2].copy()))
                 w += 2 + 2 * s2
             wn = int(wit[513 * i + 512])
-            out.append(dict(hdr=h, doms=doms[16 * i: 16 * i + int(h[8])].copy(),
-                            kids=children, wit=np.sort(wit[513 * i: 513 * i + wn].copy())))
+            d = dict(hdr=h, doms=doms[16 * i: 16 * i + int(h[8])].copy(),
+                     kids=children, wit=np.sort(wit[513 * i: 513 * i + wn].copy()))
+            if shortlist:
+                k_sl = int(sl[17 * i])
+                d["sl_ids"] = sl[17 * i + 1: 17 * i + 1 + k_sl].copy()
+                d["sl_feat"] = slf[256 * i: 256 * i + 16 * k_sl].reshape(k_sl, 16).copy()
+            out.append(d)
         return out
 
     def close(self):

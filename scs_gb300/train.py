@@ -77,6 +77,82 @@ def collect(eng, rows, max_records=8_000_000, sample_shift=2):
     return X[keep], y[keep], info
 
 
+def lookahead(eng, n, off, adj, rows, max_len=8000, per_level=3, levels=3, batch=24,
+              seed=0, log=None):
+    """Strong-branching labels from the engine's own one-step test kernel.
+
+    For each training query: its local graph is prepared, the root task and
+    a few sampled descendants (up to `levels` deep, `per_level` children of
+    each) are stepped with the shortlist on, and every shortlisted candidate
+    is then forced as u* (scs_debug_lookahead): the forced step's children
+    get one step each, and the candidate's cost is the summed live size of
+    the children that still branch -- the work left one level below that
+    choice.  Candidates of least cost are the positives; tasks whose
+    candidates all cost the same carry no preference and are dropped.
+    Returns (X, y, info)."""
+    from .engine import distance_bound, greedy_incumbent
+    rng = np.random.default_rng(seed)
+    X, Y = [], []
+    stat = {"queries": 0, "tasks": 0, "tasks_labelled": 0}
+    t0 = time.time()
+    core = eng.core_numbers()
+    for b0 in range(0, len(rows), batch):
+        kls, ubds, keep = [], [], []
+        for (l, h, q, hf, ld) in rows[b0:b0 + batch]:
+            kl, _ = greedy_incumbent(n, off, adj, l, h, q)
+            if kl >= min(int(core[q]), h - 1):
+                continue  # answered by the incumbent: never searched
+            keep.append((l, h, q, 0, ld))
+            kls.append(kl)
+            ubds.append(distance_bound(kl, h))
+        if not keep:
+            continue
+        nl, ql = eng.debug_prepare(keep, kls, ubds)
+        level = []
+        for i in range(len(keep)):
+            if 0 < int(nl[i]) <= max_len:
+                ent = np.arange(int(nl[i]), dtype=np.uint32) << 1
+                ent[int(ql[i])] |= 1
+                level.append((i, kls[i], ent))
+        stat["queries"] += len(level)
+        for _ in range(levels):
+            if not level:
+                break
+            got = eng.debug_step(level, shortlist=True)
+            nxt, lt, lf, pend = [], [], [], []
+            for task, g in zip(level, got):
+                if int(g["hdr"][0]) != 0:
+                    continue  # pruned: no branching decision here
+                kids = [k for k in g["kids"] if len(k[2]) <= max_len]
+                for j in rng.permutation(len(kids))[:per_level]:
+                    nxt.append((task[0], int(g["hdr"][1]), kids[j][2]))
+                ids = g["sl_ids"]
+                if len(ids) < 2:
+                    continue
+                lt += [task] * len(ids)
+                lf += [int(c) for c in ids]
+                pend.append((g["sl_feat"], len(ids)))
+            stat["tasks"] += len(pend)
+            if lt:
+                _, _, _, cost = eng.debug_lookahead(lt, lf)
+                k = 0
+                for feat, m in pend:
+                    c = cost[k:k + m].astype(np.float64)
+                    k += m
+                    if c.max() > c.min():
+                        X.append(feat)
+                        Y.append((c == c.min()).astype(np.float32))
+            level = nxt
+        if log:
+            log("lookahead: %d queries, %d tasks, %d labelled, %.0f s"
+                % (stat["queries"], stat["tasks"], len(Y), time.time() - t0))
+    stat["tasks_labelled"] = len(Y)
+    stat["seconds"] = round(time.time() - t0, 1)
+    if not X:
+        return np.zeros((0, 16), np.float32), np.zeros(0, np.float32), stat
+    return np.concatenate(X).astype(np.float32), np.concatenate(Y), stat
+
+
 def evaluate(eng, rows, model_path):
     """Plain vs learned on the same queries: answers, exact counts, tasks."""
     out = {}
@@ -101,10 +177,14 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--queries", type=int, default=5000)
     ap.add_argument("--heldout", type=int, default=1000)
-    ap.add_argument("--node-budget", type=int, default=100000)
+    ap.add_argument("--node-budget", type=int, default=20000)
     ap.add_argument("--epochs", type=int, default=30)
     ap.add_argument("--max-samples", type=int, default=400000)
     ap.add_argument("--sample-shift", type=int, default=2)
+    ap.add_argument("--label", default="lookahead", choices=["lookahead", "membership"],
+                    help="lookahead: strong-branching labels from forced one-step "
+                         "lookahead; membership: candidate in the returned optimum")
+    ap.add_argument("--lookahead-queries", type=int, default=400)
     ap.add_argument("--out", default=DEFAULT_OUT)
     ap.add_argument("--device", type=int, default=0)
     a = ap.parse_args()
@@ -116,7 +196,12 @@ def main():
     rows = [tuple(int(x) for x in r) for r in W.queries_mid(core, a.queries, seed=TRAIN_SEED)]
     eng = Engine(csr=(n, off, adj), limit_queries=1000, node_budget=a.node_budget,
                  device=a.device)
-    X, y, info = collect(eng, rows, sample_shift=a.sample_shift)
+    if a.label == "lookahead":
+        X, y, info = lookahead(eng, n, off, adj, rows[: a.lookahead_queries],
+                               log=lambda m: print(m, flush=True))
+    else:
+        X, y, info = collect(eng, rows, sample_shift=a.sample_shift)
+    info["label"] = a.label
     rng = np.random.default_rng(0)
     if len(y) > a.max_samples:
         idx = rng.choice(len(y), a.max_samples, replace=False)

@@ -19,6 +19,18 @@ def _gold_c1():
     return [q for q in g if q["finished"]]
 
 
+@pytest.fixture(scope="module")
+def og_c1_learned(chunglu_small, oracle_lib):
+    return oracle_lib.OracleGraph.from_file(chunglu_small)
+
+
+@pytest.fixture(scope="module")
+def eng_c1_learned(chunglu_small):
+    e = _engine(chunglu_small, limit_queries=32)
+    yield e
+    e.close()
+
+
 def _engine(graph, **kw):
     from scs_gb300.engine import Engine
     kw.setdefault("pool_words", 1 << 26)
@@ -127,3 +139,53 @@ def test_trained_network_gain_on_heldout_queries():
     # the network must not cost exact answers (within 2 % of the queries:
     # the two searches cut different trees at the same task budget)
     assert l["exact"] >= p["exact"] - 4
+
+
+def test_forced_rule_choice_and_lookahead(eng_c1_learned, og_c1_learned, oracle_lib):
+    """The one-step test kernel's forced u*: forcing the rule's own choice
+    reproduces the unforced step, the shortlist holds the rule's u*, and the
+    strong-branching lookahead counts that step's children."""
+    from scs_gb300 import workloads as W
+    og = og_c1_learned
+    cases = []
+    for (l, h, q, hf, ld) in W.queries_small(og.core).tolist():
+        kl, _ = og.heuristic(0, l, h, q)
+        if kl < min(int(og.core[q]), h - 1):
+            cases.append((l, h, q, ld, kl, int(oracle_lib.lib().orc_ubd_host(kl, h))))
+        if len(cases) == 4:
+            break
+    eng = eng_c1_learned
+    eng.debug_prepare([(l, h, q, 0, ld) for (l, h, q, ld, kl, ubd) in cases],
+                      [c[4] for c in cases], [c[5] for c in cases])
+    tasks = []
+    for i, (l, h, q, ld, kl, ubd) in enumerate(cases):
+        ctx = oracle_lib.OracleCtx(og, l, h, q, kl, ubd, ld)
+        tasks += [(i, k, e) for e, k in ctx.collect_tasks(kl, 10)]
+    base = eng.debug_step(tasks, shortlist=True)
+    branching = [j for j, g in enumerate(base) if int(g["hdr"][0]) == 0]
+    assert branching
+    force = [int(base[j]["hdr"][7]) for j in branching]
+    sub = [tasks[j] for j in branching]
+    forced = eng.debug_step(sub, force=force)
+    for j, g in zip(branching, forced):
+        b = base[j]
+        assert int(b["hdr"][7]) in set(int(x) for x in b["sl_ids"])
+        assert np.array_equal(g["hdr"][:12], b["hdr"][:12])
+        assert len(g["kids"]) == len(b["kids"])
+        for k1, k2 in zip(g["kids"], b["kids"]):
+            assert np.array_equal(k1[2], k2[2])
+        assert b["sl_feat"].shape == (len(b["sl_ids"]), 16)
+        assert np.isfinite(b["sl_feat"]).all()
+    hdr, nk, br, cost = eng.debug_lookahead(sub, force)
+    for j, i in enumerate(branching):
+        assert int(nk[j]) == len(base[i]["kids"])
+        assert int(br[j]) <= int(nk[j])
+        assert (int(cost[j]) == 0) == (int(br[j]) == 0)
+    # another shortlisted candidate as u*: still a valid branching step
+    alt = []
+    for j in branching:
+        ids = [int(x) for x in base[j]["sl_ids"]]
+        alt.append(ids[-1])
+    hdr2, nk2, br2, cost2 = eng.debug_lookahead(sub, alt)
+    for j in range(len(sub)):
+        assert int(hdr2[j][0]) == 0 and int(hdr2[j][7]) == alt[j]
