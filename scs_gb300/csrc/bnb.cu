@@ -1946,8 +1946,10 @@ step_test_kernel(SearchParams P) {
       hdr[9] = nk;
       hdr[10] = (uint32_t)w;
     }
-    clear_aux_list(T, sh);
   }
+  // the child marks of a branching step (aux words, zero between tasks) are
+  // cleared whether or not the children were written
+  if (sh.outcome == 0) clear_aux_list(T, sh);
   if (threadIdx.x == 0) {
     hdr[0] = sh.outcome;
     hdr[1] = sh.kl;
