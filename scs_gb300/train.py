@@ -1,6 +1,7 @@
 """Train the learned branching scorer from the exact solver's own traces.
 
-    python -m scs_gb300.train [--queries 5000] [--out scs_gb300/weights/rmat_s15_ef16.mlp]
+    python -m scs_gb300.train [--queries 5000] [--label membership|lookahead]
+                              [--out scs_gb300/weights/rmat_s15_ef16.mlp]
 
 1. The plain engine solves the training queries of the mid-size R-MAT
    workload (scale 15, edge factor 16; query seed 100, disjoint from the
@@ -14,6 +15,9 @@
 3. The network is trained on the GPU by the engine's own kernels
    (scs_mlp_train), positives weighted up to balance the classes, and
    written as a model file for scs_load_model.
+
+With --label lookahead, step 1-2 are replaced by strong-branching labels
+from the engine's one-step test kernel (see lookahead()).
 
 The file written here is the one the benchmark's learned arm loads.
 """
@@ -177,11 +181,13 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--queries", type=int, default=5000)
     ap.add_argument("--heldout", type=int, default=1000)
-    ap.add_argument("--node-budget", type=int, default=20000)
+    ap.add_argument("--node-budget", type=int, default=100000,
+                    help="task budget of the trace run and the held-out evaluation "
+                         "(the committed model: 100000)")
     ap.add_argument("--epochs", type=int, default=30)
     ap.add_argument("--max-samples", type=int, default=400000)
     ap.add_argument("--sample-shift", type=int, default=2)
-    ap.add_argument("--label", default="lookahead", choices=["lookahead", "membership"],
+    ap.add_argument("--label", default="membership", choices=["membership", "lookahead"],
                     help="lookahead: strong-branching labels from forced one-step "
                          "lookahead; membership: candidate in the returned optimum")
     ap.add_argument("--lookahead-queries", type=int, default=400)
