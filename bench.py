@@ -16,9 +16,11 @@ best degree found with status "timeout" (the reference's Overtime=1) and
 does not count as exact.
 
 value  = exact answers (status done or heuristic) / device time of the
-         timed steps (CUDA events on the engine's stream around submit, run
-         and poll; graph resident).  Budget-stopped answers are not counted;
-         all answers per second are reported beside it in config.
+         timed steps (CUDA events recorded around submit, run and poll; the
+         engine's own stream is synchronized before the call returns; graph
+         resident).  Budget-stopped answers are not counted; all answers per
+         second are reported beside it in config.  Default budget: 20,000
+         search tasks per query.
 e2e    = exact answers / host-clock time of the same calls through the C
          ABI from host buffers (submit, run, poll of results and
          communities).  The engine is host-driven between slices, so the two
@@ -28,6 +30,11 @@ branch-and-bound on the reference's heuristics) on all host cores, on a
 sample of each step's queries under the same node budget, no wall cap.
 --serve RATES runs Poisson arrivals at each rate (queries/s) instead and
 prints one line per rate with latency from arrival (see run_serve).
+--arm plain|learned picks the integer rules alone (default) or the trained
+network's branching and incumbent proposal; the other arm is run on the
+first step's queries after the timed region and reported in config.compare.
+--workload chunglu_n1m / rmat_s22 selects the 1M-vertex Chung-Lu workload or
+the scale-22 R-MAT serving workload instead of the mid-size one.
 """
 import argparse
 import json
