@@ -2,7 +2,7 @@
  * oracle.h -- CPU restatement of the size-bounded community search (SCS)
  * hot path of wajidmanzoor/SCS.  TEST INFRASTRUCTURE ONLY: only tests/,
  * __graft_entry__.smoke() and bench.py's CPU-baseline legs load this library,
- * always as the checker, never as the measured or shipped path.
+ * always to check or time against, never as the measured or shipped path.
  *
  * Parity status: the graph loader, core numbers, BFS and the three greedy
  * heuristics are pinned bit-exactly against the reference's own CPU code

@@ -1,4 +1,4 @@
-"""The answer checker (scs_check_community) and the scs_verify CLI.
+"""The answer verifier (scs_check_community) and the scs_verify CLI.
 
 The reference reports only the degree of an answer (main.cu:328-334); the
 engine also returns the community, and these tests pin the checks applied to
