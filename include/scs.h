@@ -128,7 +128,9 @@ typedef struct scs_engine scs_engine;
 int scs_create(scs_engine **out, const char *edge_list_path,
                const scs_config *cfg);
 
-/* Create from a symmetric CSR with ascending neighbour lists. */
+/* Create from a symmetric CSR with strictly ascending neighbour lists and no
+ * self-loops (the form scs_read_edge_list returns).  Returns SCS_EINVAL when
+ * the CSR breaks one of these, e.g. an edge listed in only one of its rows. */
 int scs_create_csr(scs_engine **out, uint32_t n, const uint32_t *off,
                    const uint32_t *adj, const scs_config *cfg);
 
@@ -229,7 +231,11 @@ int scs_core_decompose_gpu(uint32_t n, const uint32_t *off, const uint32_t *adj,
                            uint32_t *core, int device);
 
 /* Greedy incumbent kl = max(heu2, heu3, heu4) and its community
- * (CSSC_heu, inc/heuristic.h:321-349).  H needs room for max(h, deg(q)+1). */
+ * (CSSC_heu, inc/heuristic.h:321-349).  H needs room for max(h, deg(q)+1).
+ * The CSR is checked as for scs_create_csr (SCS_EINVAL).  The counts and
+ * scores the reference recomputes by rescanning neighbour rows are kept up to
+ * date instead, with the same values and pop order, so kl and H are the
+ * reference's. */
 int scs_greedy_incumbent(uint32_t n, const uint32_t *off, const uint32_t *adj,
                          uint32_t l, uint32_t h, uint32_t q, uint32_t *kl,
                          uint32_t *H, uint32_t *hsize);

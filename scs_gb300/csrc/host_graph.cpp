@@ -197,6 +197,28 @@ int adopt_csr(uint32_t n, const uint32_t *off, const uint32_t *adj,
       }
     }
   }
+  // Every edge must be listed in both of its rows: the counts of the greedy
+  // incumbent and of the search are taken from either side.
+  std::atomic<bool> asym{false};
+  unsigned nt = off[n] < (1u << 20) ? 1u
+                                    : std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  std::vector<std::thread> th;
+  for (unsigned k = 0; k < nt; k++)
+    th.emplace_back([&, k]() {
+      for (uint32_t i = k; i < n && !asym.load(std::memory_order_relaxed); i += nt)
+        for (uint32_t e = off[i]; e < off[i + 1]; e++) {
+          uint32_t j = adj[e];
+          if (!std::binary_search(adj + off[j], adj + off[j + 1], i)) {
+            asym.store(true, std::memory_order_relaxed);
+            break;
+          }
+        }
+    });
+  for (auto &t : th) t.join();
+  if (asym.load()) {
+    err = "CSR not symmetric: an edge is missing from one of its rows";
+    return -1;
+  }
   g.n = n;
   g.off.assign(off, off + n + 1);
   g.adj.assign(adj, adj + off[n]);
@@ -260,6 +282,7 @@ void HeuWork::ensure(uint32_t n) {
   if (sta.size() < n) {
     sta.assign(n, 0);
     deg.assign(n, 0);
+    slot.assign(n, 0);
     inS.assign(n, 0);
   }
   touched.clear();
@@ -290,14 +313,25 @@ namespace {
 constexpr uint32_t HEU_INF = 1000000000u;
 
 // heu2: grow from q, always taking the frontier vertex with most neighbours
-// inside H (ties to the larger id)
+// inside H (ties to the larger id).
+//
+// The reference recounts |N(x) & H| by a scan of N(x) for every neighbour x
+// of every vertex that joins H, which costs sum deg(v) * deg(x) and takes
+// seconds per query on graphs with hubs.  Here cnt[x] = |N(x) & H| is kept
+// for every vertex: a vertex joining H adds one to each of its neighbours
+// (the graph is symmetric with unique rows, which adopt_csr and the loader
+// guarantee), so the count pushed for x is the same number the scan gives.
+// For a member of H the same count is its degree inside H.  The queue holds
+// the same (count, id) pairs, so the pop order, kl and H are unchanged.
 uint32_t heu2(const HostGraph &g, uint32_t N1, uint32_t N2, uint32_t q,
               HeuWork &w, std::vector<uint32_t> &H) {
   const uint32_t *off = g.off.data(), *adj = g.adj.data();
   auto &sta = w.sta;
-  auto &deg = w.deg;
-  std::vector<uint32_t> touched;
-  std::vector<uint32_t> tH;
+  auto &cnt = w.deg;
+  auto &touched = w.touched;
+  auto &tH = w.tH;
+  touched.clear();
+  tH.clear();
   uint32_t tkl = 0, tsz = 0;
   std::priority_queue<std::pair<uint32_t, uint32_t>> Q;
   Q.push({0, q});
@@ -309,72 +343,11 @@ uint32_t heu2(const HostGraph &g, uint32_t N1, uint32_t N2, uint32_t q,
     if (sta[v] == 2) continue;
     tH.push_back(v);
     sta[v] = 2;
-    for (uint32_t j = off[v]; j < off[v + 1]; j++) {
-      uint32_t x = adj[j];
-      if (sta[x] == 0 || sta[x] == 1) {
-        uint32_t d = 0;
-        for (uint32_t k = off[x]; k < off[x + 1]; k++) d += sta[adj[k]] == 2;
-        Q.push({d, x});
-        if (sta[x] == 0) {
-          sta[x] = 1;
-          touched.push_back(x);
-        }
-      } else {
-        ++deg[x];
-        ++deg[v];
-      }
-    }
-    if (tH.size() >= N1) {
-      uint32_t md = HEU_INF;
-      for (uint32_t x : tH) md = std::min(md, deg[x]);
-      if (md >= tkl) {
-        tkl = md;
-        tsz = (uint32_t)tH.size();
-      }
-    }
-    if (tH.size() == N2) break;
-  }
-  H.assign(tH.begin(), tH.begin() + tsz);
-  for (uint32_t x : touched) sta[x] = 0;
-  for (uint32_t x : tH) deg[x] = 0;
-  return tkl;
-}
-
-// heu3: as heu2 with the connection score sum 1/deg_H(w) + degree/dMAX
-uint32_t heu3(const HostGraph &g, uint32_t N1, uint32_t N2, uint32_t q,
-              HeuWork &w, std::vector<uint32_t> &H) {
-  const uint32_t *off = g.off.data(), *adj = g.adj.data();
-  const double dM = (double)g.dmax;
-  auto &sta = w.sta;
-  auto &deg = w.deg;
-  std::vector<uint32_t> touched;
-  std::vector<uint32_t> tH;
-  uint32_t tkl = 0, tsz = 0;
-  std::priority_queue<std::pair<double, uint32_t>> Q;
-  Q.push({0.0, q});
-  sta[q] = 1;
-  touched.push_back(q);
-  while (!Q.empty()) {
-    uint32_t v = Q.top().second;
-    Q.pop();
-    if (sta[v] == 2) continue;
-    tH.push_back(v);
-    sta[v] = 2;
-    for (uint32_t j = off[v]; j < off[v + 1]; j++)
-      if (sta[adj[j]] == 2) {
-        ++deg[adj[j]];
-        ++deg[v];
-      }
+    for (uint32_t j = off[v]; j < off[v + 1]; j++) ++cnt[adj[j]];
     for (uint32_t j = off[v]; j < off[v + 1]; j++) {
       uint32_t x = adj[j];
       if (sta[x] == 2) continue;
-      double sc = 0;
-      for (uint32_t k = off[x]; k < off[x + 1]; k++) {
-        uint32_t y = adj[k];
-        if (sta[y] == 2 && deg[y] != 0) sc += (double)1 / deg[y];
-      }
-      sc += (double)g.degree[x] / dM;
-      Q.push({sc, x});
+      Q.push({cnt[x], x});
       if (sta[x] == 0) {
         sta[x] = 1;
         touched.push_back(x);
@@ -382,6 +355,113 @@ uint32_t heu3(const HostGraph &g, uint32_t N1, uint32_t N2, uint32_t q,
     }
     if (tH.size() >= N1) {
       uint32_t md = HEU_INF;
+      for (uint32_t x : tH) md = std::min(md, cnt[x]);
+      if (md >= tkl) {
+        tkl = md;
+        tsz = (uint32_t)tH.size();
+      }
+    }
+    if (tH.size() == N2) break;
+  }
+  H.assign(tH.begin(), tH.begin() + tsz);
+  for (uint32_t x : touched) {
+    sta[x] = 0;
+    cnt[x] = 0;
+  }
+  return tkl;
+}
+
+// heu3: as heu2 with the connection score sum 1/deg_H(y) over the members y
+// of H adjacent to x, plus degree/dMAX.
+//
+// The reference rescans N(x) for each candidate x, summing in adjacency
+// order, i.e. by ascending y (rows are ascending).  Here each candidate keeps
+// its members of H in ascending order in a 64-byte record (spilling to a
+// vector past HeuRec::INLINE), extended when a neighbour joins H, and the sum
+// runs over that list: the same terms added in the same order, so every score
+// is bit-identical.  A candidate enters the queue only when its score beats
+// the best one it already holds there: an entry at or below that is popped
+// after it (the pairs order by score, then id), when the candidate is already
+// in H, so the pop order is the reference's.
+uint32_t heu3(const HostGraph &g, uint32_t N1, uint32_t N2, uint32_t q,
+              HeuWork &w, std::vector<uint32_t> &H) {
+  const uint32_t *off = g.off.data(), *adj = g.adj.data();
+  const double dM = (double)g.dmax;
+  constexpr uint32_t IN_H = 1;  // st[x]: 0 untouched, 1 in H, r + 2 record r
+  auto &st = w.slot;
+  auto &deg = w.deg;
+  auto &recs = w.recs;
+  auto &touched = w.touched;
+  auto &tH = w.tH;
+  auto &cand = w.cand;
+  touched.clear();
+  tH.clear();
+  uint32_t nrec = 0, nspill = 0;
+  auto new_record = [&](uint32_t x) {
+    if (nrec == recs.size()) recs.emplace_back();
+    HeuRec &r = recs[nrec];
+    r.len = 0;
+    r.spill = 0;
+    r.best = -1.0;
+    r.dterm = (double)g.degree[x] / dM;
+    st[x] = nrec + 2;
+    touched.push_back(x);
+    return nrec++;
+  };
+  uint32_t tkl = 0, tsz = 0;
+  std::priority_queue<std::pair<double, uint32_t>> Q;
+  Q.push({0.0, q});
+  new_record(q);
+  while (!Q.empty()) {
+    uint32_t v = Q.top().second;
+    Q.pop();
+    if (st[v] == IN_H) continue;
+    tH.push_back(v);
+    st[v] = IN_H;
+    // degrees inside H first: every score below reads them
+    cand.clear();
+    for (uint32_t j = off[v]; j < off[v + 1]; j++) {
+      uint32_t x = adj[j], sx = st[x];
+      if (sx == IN_H) {
+        ++deg[x];
+        ++deg[v];
+      } else {
+        cand.push_back(x);
+        cand.push_back(sx ? sx - 2 : new_record(x));
+      }
+    }
+    for (size_t c = 0; c < cand.size(); c += 2) {
+      uint32_t x = cand[c];
+      HeuRec &r = recs[cand[c + 1]];
+      double sc = 0;
+      if (!r.spill && r.len < HeuRec::INLINE) {
+        uint32_t i = r.len++;
+        while (i > 0 && r.ids[i - 1] > v) {
+          r.ids[i] = r.ids[i - 1];
+          i--;
+        }
+        r.ids[i] = v;
+        for (uint32_t k = 0; k < r.len; k++)
+          if (deg[r.ids[k]] != 0) sc += (double)1 / deg[r.ids[k]];
+      } else {
+        if (!r.spill) {
+          if (nspill == w.spills.size()) w.spills.emplace_back();
+          w.spills[nspill].assign(r.ids, r.ids + r.len);
+          r.spill = ++nspill;
+        }
+        auto &L = w.spills[r.spill - 1];
+        L.insert(std::upper_bound(L.begin(), L.end(), v), v);
+        for (uint32_t y : L)
+          if (deg[y] != 0) sc += (double)1 / deg[y];
+      }
+      sc += r.dterm;
+      if (sc > r.best) {
+        r.best = sc;
+        Q.push({sc, x});
+      }
+    }
+    if (tH.size() >= N1) {
+      uint32_t md = HEU_INF;
       for (uint32_t x : tH) md = std::min(md, deg[x]);
       if (md >= tkl) {
         tkl = md;
@@ -391,7 +471,7 @@ uint32_t heu3(const HostGraph &g, uint32_t N1, uint32_t N2, uint32_t q,
     if (tH.size() == N2) break;
   }
   H.assign(tH.begin(), tH.begin() + tsz);
-  for (uint32_t x : touched) sta[x] = 0;
+  for (uint32_t x : touched) st[x] = 0;
   for (uint32_t x : tH) deg[x] = 0;
   return tkl;
 }

@@ -20,15 +20,30 @@ struct HostGraph {
 // Returns 0, or a negative code with a message in err.
 // with_core = false leaves g.core empty (the engine computes it on the GPU).
 int load_edge_list(const char *path, HostGraph &g, std::string &err, bool with_core = true);
-// Validate a caller CSR and adopt it.
+// Validate a caller CSR (rows strictly ascending, no self-loops, every edge in
+// both rows) and adopt it.
 int adopt_csr(uint32_t n, const uint32_t *off, const uint32_t *adj,
               HostGraph &g, std::string &err, bool with_core = true);
 // Degrees, dmax and (with_core) core numbers by bin-sort peeling.
 void finish_graph(HostGraph &g, bool with_core = true);
 
+// heu3's per-candidate record: its members of H in ascending id order
+// (inline up to INLINE, else in HeuWork::spills[spill - 1]), the best score
+// it holds in the queue, and its degree/dMAX term.  One cache line.
+struct alignas(64) HeuRec {
+  static constexpr uint32_t INLINE = 10;
+  uint32_t len, spill;
+  double best, dterm;
+  uint32_t ids[INLINE];
+};
+
 // Per-thread work arrays for the greedy incumbent; reused across queries.
 struct HeuWork {
   std::vector<uint32_t> sta, deg, tH, touched;
+  std::vector<uint32_t> slot;  // heu3: 0 untouched, 1 in H, r + 2 record r
+  std::vector<uint32_t> cand;  // heu3: (candidate, record) pairs of one pop
+  std::vector<HeuRec> recs;
+  std::vector<std::vector<uint32_t>> spills;
   std::vector<uint8_t> inS;
   void ensure(uint32_t n);
 };
