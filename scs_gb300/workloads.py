@@ -21,13 +21,21 @@ GRAPH_SEED = 1234
 QUERY_SEED = 42
 
 
+def _sorted_unique(a):
+    """np.unique of an int64 array (ascending, no repeats) by one sort."""
+    a = np.sort(a, kind="stable")
+    keep = np.ones(a.size, dtype=bool)
+    np.not_equal(a[1:], a[:-1], out=keep[1:])
+    return a[keep]
+
+
 def _dedup_pairs(u, v):
     """Canonical (min, max) pairs without self-loops, unique, as int64 keys."""
     keep = u != v
     u, v = u[keep], v[keep]
     lo = np.minimum(u, v).astype(np.int64)
     hi = np.maximum(u, v).astype(np.int64)
-    return np.unique(lo * (1 << 32) + hi)
+    return _sorted_unique(lo * (1 << 32) + hi)
 
 
 def _top_up(sampler, m, rng, batch):
@@ -38,7 +46,8 @@ def _top_up(sampler, m, rng, batch):
     while keys.size < m:
         u, v = sampler(rng, batch)
         new = _dedup_pairs(u, v)
-        keys = np.union1d(keys, new) if keys.size else new
+        # union of two ascending runs: the stable sort merges them
+        keys = _sorted_unique(np.concatenate([keys, new])) if keys.size else new
         rounds += 1
         if rounds > 10000:
             raise RuntimeError("generator cannot reach the requested edge count")
@@ -96,8 +105,8 @@ def rmat(scale, m, a=0.57, b=0.19, c=0.19, seed=GRAPH_SEED):
         v = np.zeros(batch, dtype=np.int64)
         for bit in range(scale):
             x = r.random(batch)
-            q = np.searchsorted(cum, x, side="right")
-            q = np.minimum(q, 3)
+            # quadrant = number of cumulative bounds <= x, at most 3
+            q = (x >= cum[0]).astype(np.int64) + (x >= cum[1]) + (x >= cum[2])
             u |= ((q >> 1) & 1).astype(np.int64) << bit
             v |= (q & 1).astype(np.int64) << bit
         return perm[u], perm[v]
