@@ -101,6 +101,7 @@ struct scs_engine {
   std::vector<SlotHost> slots;
   // prep
   uint32_t prep_cap = 0;
+  uint32_t prep_cluster = 1;  // CTAs per query in preparation (prep.cu)
   PrepScratch ps{};
   PrepJob *d_jobs = nullptr;
   // search
@@ -275,6 +276,15 @@ static int engine_init(scs_engine *E) {
   PrepScratch &ps = E->ps;
   ps.stride_n = n;
   ps.stride_w = (n + 31) / 32 + 1;
+  ps.big_row = c.prep_big_row ? c.prep_big_row : 4096;
+  // a cluster per query on large graphs, where one SM's BFS and compaction
+  // over the CSR would take a large share of the query's time
+  E->prep_cluster = c.prep_ctas ? c.prep_ctas : (n >= (1u << 18) ? PREP_MAX_CLUSTER : 1u);
+  if (E->prep_cluster != 1 && E->prep_cluster != 2 && E->prep_cluster != 4 &&
+      E->prep_cluster != 8) {
+    E->err = "prep_ctas must be 1, 2, 4 or 8";
+    return SCS_EINVAL;
+  }
   RC(E->dalloc(&ps.dist, (size_t)E->prep_cap * n, false));
   RC(E->dalloc(&ps.vis, (size_t)E->prep_cap * ps.stride_w, false));
   RC(E->dalloc(&ps.comp, (size_t)E->prep_cap * ps.stride_w, false));
@@ -554,10 +564,9 @@ static int admit(scs_engine *E) {
   if (e != cudaSuccess) return requeue(e, "prep job copy");
   e = cudaEventRecord(E->ev2, E->stream);
   if (e != cudaSuccess) return requeue(e, "prep start event");
-  prep_kernel<<<(unsigned)jobs.size(), PREP_THREADS, 0, E->stream>>>(
-      DevGraph{E->g.n, E->g.dmax, E->d_off, E->d_adj, E->d_core}, E->sa, E->d_slots,
-      E->d_jobs, (int)jobs.size(), E->ps, E->pool, E->d_ctr);
-  e = cudaGetLastError();
+  e = launch_prep(E->prep_cluster, E->stream,
+                  DevGraph{E->g.n, E->g.dmax, E->d_off, E->d_adj, E->d_core}, E->sa,
+                  E->d_slots, E->d_jobs, (int)jobs.size(), E->ps, E->pool, E->d_ctr);
   if (e != cudaSuccess) return requeue(e, "prep_kernel launch");
   if (E->learned) {
     // the network's incumbent proposal on each new local graph (propose.cu)
@@ -1095,10 +1104,9 @@ int scs_debug_prepare(scs_engine *E, uint32_t nq, const scs_query *qs,
   }
   CK(cudaMemcpyAsync(E->d_jobs, jobs.data(), nq * sizeof(PrepJob),
                      cudaMemcpyHostToDevice, E->stream));
-  prep_kernel<<<nq, PREP_THREADS, 0, E->stream>>>(
-      DevGraph{E->g.n, E->g.dmax, E->d_off, E->d_adj, E->d_core}, E->sa,
-      E->d_slots, E->d_jobs, (int)nq, E->ps, E->pool, E->d_ctr);
-  CK(cudaGetLastError());
+  CK(launch_prep(E->prep_cluster, E->stream,
+                 DevGraph{E->g.n, E->g.dmax, E->d_off, E->d_adj, E->d_core}, E->sa,
+                 E->d_slots, E->d_jobs, (int)nq, E->ps, E->pool, E->d_ctr));
   CK(cudaMemcpyAsync(E->h_slots.data(), E->d_slots, nq * sizeof(Slot),
                      cudaMemcpyDeviceToHost, E->stream));
   CK(cudaStreamSynchronize(E->stream));

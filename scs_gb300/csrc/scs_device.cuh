@@ -185,6 +185,7 @@ struct PrepScratch {
   uint32_t *wpre;  // [jobs][nw+1]
   uint32_t stride_n;
   uint32_t stride_w;
+  uint32_t big_row;  // rows this long are walked by a whole CTA (prep.cu)
 };
 
 struct SearchParams {
@@ -249,9 +250,12 @@ constexpr int PREP_THREADS = 512;
 constexpr int SEARCH_THREADS = SCS_SEARCH_THREADS;
 constexpr int SEARCH_MINB = SCS_SEARCH_MINB;
 
-__global__ void prep_kernel(DevGraph g, SlotArrays sa, Slot *slots,
-                            const PrepJob *jobs, int njobs, PrepScratch ps,
-                            Pool pool, Counters *ctr);
+// Per-query preparation: one thread-block cluster of `cluster` CTAs (1, 2, 4
+// or 8) per job; prep.cu.
+constexpr uint32_t PREP_MAX_CLUSTER = 8;
+cudaError_t launch_prep(uint32_t cluster, cudaStream_t stream, DevGraph g,
+                        SlotArrays sa, Slot *slots, const PrepJob *jobs,
+                        int njobs, PrepScratch ps, Pool pool, Counters *ctr);
 __global__ void search_kernel(SearchParams P);
 // the same search with the learned branching choice and the trace
 __global__ void search_kernel_learned(SearchParams P);

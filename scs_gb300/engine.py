@@ -38,7 +38,8 @@ class Config(C.Structure):
                 ("node_budget", C.c_uint64), ("host_threads", C.c_uint32),
                 ("device", C.c_int32), ("active_queries", C.c_uint32),
                 ("release_order", C.c_uint32), ("release_headroom", C.c_uint32),
-                ("max_local", C.c_uint32), ("host_release_only", C.c_uint32)]
+                ("max_local", C.c_uint32), ("host_release_only", C.c_uint32),
+                ("prep_ctas", C.c_uint32), ("prep_big_row", C.c_uint32)]
 
 
 class Query(C.Structure):
@@ -310,7 +311,8 @@ class Engine:
     def __init__(self, graph=None, csr=None, limit_queries=64, rules=None,
                  slice_us=0, node_budget=0, ctas_per_sm=0, stack_words=0,
                  pool_words=0, host_threads=0, device=0, active_queries=0,
-                 release_order=0, release_headroom=0, max_local=0, host_release_only=0):
+                 release_order=0, release_headroom=0, max_local=0, host_release_only=0,
+                 prep_ctas=0, prep_big_row=0):
         L = lib()
         cfg = Config()
         cfg.limit_queries = limit_queries
@@ -326,6 +328,8 @@ class Engine:
         cfg.release_headroom = release_headroom
         cfg.max_local = max_local
         cfg.host_release_only = host_release_only
+        cfg.prep_ctas = prep_ctas
+        cfg.prep_big_row = prep_big_row
         if rules is not None:
             cfg.rules_set = 1
             cfg.red1, cfg.red2, cfg.red3, cfg.prun1, cfg.prun2 = [int(bool(r)) for r in rules]

@@ -72,6 +72,73 @@ def test_prepare_parity(eng_c1, og_c1, oracle_lib):
         assert np.array_equal(dist, ctx.dist)
 
 
+@pytest.mark.parametrize("ctas,big_row", [(2, 4096), (8, 4096), (8, 16), (4, 64), (1, 16)])
+def test_cluster_prepare_parity(chunglu_small, og_c1, oracle_lib, ctas, big_row):
+    """Preparation by a cluster of CTAs per query gives the oracle's local
+    graph bit for bit, with rows of at least big_row entries walked by whole
+    CTAs (16 and 64 make most rows of this graph such rows)."""
+    cases = _prep_cases(og_c1, oracle_lib, 24)
+    qs = [(l, h, q, 0, ld) for (l, h, q, ld, kl, ubd) in cases]
+    eng = _engine(graph=chunglu_small, limit_queries=len(cases), prep_ctas=ctas,
+                  prep_big_row=big_row)
+    try:
+        nl, ql = eng.debug_prepare(qs, [c[4] for c in cases], [c[5] for c in cases])
+        for i, (l, h, q, ld, kl, ubd) in enumerate(cases):
+            ctx = oracle_lib.OracleCtx(og_c1, l, h, q, kl, ubd, ld)
+            assert int(nl[i]) == ctx.n and int(ql[i]) == ctx.q_local
+            gid, off, adj, dist = eng.debug_local_graph(i, int(nl[i]), int(ctx.off[-1]) + 8)
+            assert np.array_equal(gid, ctx.gid)
+            assert np.array_equal(off, ctx.off)
+            assert np.array_equal(adj, ctx.adj)
+            assert np.array_equal(dist, ctx.dist)
+    finally:
+        eng.close()
+
+
+def test_cluster_prepare_rmat_hubs(rmat15, oracle_lib):
+    """The same on the R-MAT graph, whose hubs (up to 6,085 neighbours) take
+    the whole-CTA path at the default row threshold, with 8 CTAs per query."""
+    og = oracle_lib.OracleGraph.from_file(rmat15)
+    from scs_gb300 import workloads as W
+    cases = []
+    for (l, h, q, hf, ld) in W.queries_mid(og.core)[:40].tolist():
+        kl, _ = og.heuristic(0, l, h, q)
+        if kl >= min(int(og.core[q]), h - 1):
+            continue
+        cases.append((l, h, q, ld, kl, int(oracle_lib.lib().orc_ubd_host(kl, h))))
+    cases = cases[:16]
+    assert len(cases) >= 8
+    qs = [(l, h, q, 0, ld) for (l, h, q, ld, kl, ubd) in cases]
+    eng = _engine(graph=rmat15, limit_queries=len(cases), prep_ctas=8)
+    try:
+        nl, ql = eng.debug_prepare(qs, [c[4] for c in cases], [c[5] for c in cases])
+        for i, (l, h, q, ld, kl, ubd) in enumerate(cases):
+            ctx = oracle_lib.OracleCtx(og, l, h, q, kl, ubd, ld)
+            assert int(nl[i]) == ctx.n and int(ql[i]) == ctx.q_local
+            gid, off, adj, dist = eng.debug_local_graph(i, int(nl[i]), int(ctx.off[-1]) + 8)
+            assert np.array_equal(gid, ctx.gid)
+            assert np.array_equal(off, ctx.off)
+            assert np.array_equal(adj, ctx.adj)
+            assert np.array_equal(dist, ctx.dist)
+    finally:
+        eng.close()
+
+
+def test_cluster_prepare_keeps_answers(chunglu_small, og_c1):
+    """Whole searches on local graphs prepared by 8-CTA clusters (rows of 32
+    or more entries by whole CTAs) give the golden exact answers."""
+    gold = [g for g in _golden_c1()["queries"] if g["finished"]]
+    rows = [(g["l"], g["h"], g["q"], g["heur"], g["limit_doms"]) for g in gold]
+    eng = _engine(graph=chunglu_small, limit_queries=64, prep_ctas=8, prep_big_row=32)
+    try:
+        res = eng.solve(rows)
+    finally:
+        eng.close()
+    for g, r in zip(gold, res):
+        assert r["status"] in (0, 1), r
+        assert r["degree"] == g["degree"], (g, r)
+
+
 def _compare_steps(eng, ctxs, tasks):
     """tasks: list of (slot, kl, entries); ctxs: slot -> OracleCtx."""
     got = eng.debug_step(tasks)
