@@ -567,6 +567,11 @@ def main():
                    "proposals_better": st1["proposals_better"] - st0["proposals_better"],
                    "device_releases": st1["device_releases"] - st0["device_releases"],
                    "host_release_only": bool(args.host_release_only),
+                   # engine time over the timed steps: preparation launches,
+                   # search slices, and admission waiting on host incumbents
+                   # with nothing searching
+                   "engine_ms": {k: (st1[k + "_ns"] - st0[k + "_ns"]) / 1e6
+                                 for k in ("prep", "search", "heur")},
                    "compare": compare},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak if peak else None, "traffic": traffic,
