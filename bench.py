@@ -300,7 +300,8 @@ def run_serve(args):
                      slice_us=args.slice_us or 5000,
                      ctas_per_sm=args.ctas_per_sm, node_budget=args.node_budget,
                      stack_words=args.stack_words, pool_words=args.pool_words, device=local,
-                     active_queries=args.active_queries, max_local=args.max_local)
+                     active_queries=args.active_queries, max_local=args.max_local,
+                     prep_ctas=args.prep_ctas)
         if args.arm == "learned":
             eng.load_model(args.model)
         eng.solve([tuple(int(x) for x in r) for r in queries_for(core, 8, 46)])  # warm-up
@@ -392,6 +393,8 @@ def main():
     ap.add_argument("--stack-words", type=int, default=0,
                     help="task-stack words per CTA (0: sized from device memory)")
     ap.add_argument("--pool-words", type=int, default=0)
+    ap.add_argument("--prep-ctas", type=int, default=0,
+                    help="CTAs per query in preparation (one cluster; 0: the engine's choice)")
     ap.add_argument("--clocks-csv", default=os.path.join(tempfile.gettempdir(), "scs_clocks_r%d.csv"),
                     help="where the nvidia-smi clock samples of the timed region go (%%d: rank)")
     ap.add_argument("--serve", default="",
@@ -432,7 +435,8 @@ def main():
                  node_budget=args.node_budget, stack_words=tune["stack_words"],
                  pool_words=args.pool_words, device=local,
                  active_queries=tune["active_queries"], release_order=args.release_order,
-                 max_local=args.max_local, host_release_only=int(args.host_release_only))
+                 max_local=args.max_local, host_release_only=int(args.host_release_only),
+                 prep_ctas=args.prep_ctas)
     arm = args.arm
     if arm == "auto":  # the model is trained on the mid-size workload
         arm = "learned" if os.path.exists(args.model) and args.workload == "rmat_s15" else "plain"

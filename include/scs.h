@@ -96,9 +96,10 @@ typedef struct {
                                  which releases one each time a searched
                                  query finishes */
   uint32_t prep_ctas;         /* CTAs that build one query's local graph, as
-                                 one thread-block cluster: 1, 2, 4 or 8
-                                 (0: 8 on graphs of 2^18 vertices or more,
-                                 else 1).  The output is the same for any. */
+                                 one thread-block cluster: 1, 2, 4, 8 or 16
+                                 (16 is a non-portable cluster size; 0: 8 on
+                                 graphs of 2^18 vertices or more, else 1).
+                                 The output is the same for any. */
   uint32_t prep_big_row;      /* preparation walks rows of at least this
                                  many entries with a whole CTA, shorter ones
                                  with a warp (0: 4096) */

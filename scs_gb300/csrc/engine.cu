@@ -281,8 +281,8 @@ static int engine_init(scs_engine *E) {
   // over the CSR would take a large share of the query's time
   E->prep_cluster = c.prep_ctas ? c.prep_ctas : (n >= (1u << 18) ? PREP_MAX_CLUSTER : 1u);
   if (E->prep_cluster != 1 && E->prep_cluster != 2 && E->prep_cluster != 4 &&
-      E->prep_cluster != 8) {
-    E->err = "prep_ctas must be 1, 2, 4 or 8";
+      E->prep_cluster != 8 && E->prep_cluster != 16) {
+    E->err = "prep_ctas must be 1, 2, 4, 8 or 16";
     return SCS_EINVAL;
   }
   RC(E->dalloc(&ps.dist, (size_t)E->prep_cap * n, false));

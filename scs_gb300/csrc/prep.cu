@@ -127,17 +127,20 @@ __device__ uint32_t cluster_excl_scan(cg::cluster_group &cl, PrepSh &sh,
   return total;
 }
 
-// One warp's share of a row: lanes test 32 neighbours at a time.  Appends
-// the newly reached ones to the next frontier (small ones from the front,
-// those of big_row or more neighbours from the back) and records distances
-// in mode 0.  k0 is warp-uniform.
-__device__ __forceinline__ void bfs_visit32(const DevGraph &g, uint32_t k0,
-                                            uint32_t hi, int mode, uint32_t level,
-                                            uint32_t kl, uint32_t ubd, uint32_t big_row,
-                                            uint16_t *dist,
-                                            uint32_t *vis, uint32_t *nxt, uint32_t *ncnt) {
+// Rows of at most GROUP_ROW entries are walked four at a time per warp, by
+// groups of 8 lanes, so a warp has four rows' loads in flight.
+constexpr uint32_t GROUP_ROW = 64;
+
+// Each lane tests adjacency entry k of its row (none when k >= hi; the call
+// is warp-wide).  Appends the newly reached vertices to the next frontier
+// (small ones from the front, those of big_row or more neighbours from the
+// back) and records distances in mode 0.
+__device__ __forceinline__ void bfs_visit(const DevGraph &g, uint32_t k,
+                                          uint32_t hi, int mode, uint32_t level,
+                                          uint32_t kl, uint32_t ubd, uint32_t big_row,
+                                          uint16_t *dist,
+                                          uint32_t *vis, uint32_t *nxt, uint32_t *ncnt) {
   const int lane = threadIdx.x & 31;
-  const uint32_t k = k0 + lane;
   bool fresh = false, big = false;
   uint32_t w = 0;
   if (k < hi) {
@@ -204,22 +207,38 @@ __device__ void cluster_bfs(cg::cluster_group &cl, PrepSh &sh, PrepSh *r0,
       const uint32_t lo = g.off[v], hi = g.off[v + 1];
       if (t == 0) edges += hi - lo;
       for (uint32_t k0 = lo + (uint32_t)wid * 32u; k0 < hi; k0 += PREP_THREADS)
-        bfs_visit32(g, k0, hi, mode, level, kl, ubd, big_row, dist, vis, nxt, ncnt);
+        bfs_visit(g, k0 + lane, hi, mode, level, kl, ubd, big_row, dist, vis, nxt, ncnt);
     }
-    // the others: a warp each
-    for (uint32_t fi = r * PREP_WARPS + wid; fi < ns; fi += R * PREP_WARPS) {
-      const uint32_t v = __ldcg(cur + fi);
-      const uint32_t lo = g.off[v], hi = g.off[v + 1];
-      if (lane == 0) edges += hi - lo;
-      for (uint32_t k0 = lo; k0 < hi; k0 += 32)
-        bfs_visit32(g, k0, hi, mode, level, kl, ubd, big_row, dist, vis, nxt, ncnt);
+    // the others: four per warp, by 8-lane groups when all four rows are
+    // short, else one after the other by the whole warp
+    for (uint32_t f0 = (r * PREP_WARPS + wid) * 4u; f0 < ns; f0 += R * PREP_WARPS * 4u) {
+      const uint32_t grp = lane >> 3, sl = lane & 7;
+      uint32_t lo = 0, hi = 0;
+      if (f0 + grp < ns) {
+        const uint32_t v = __ldcg(cur + f0 + grp);
+        lo = g.off[v];
+        hi = g.off[v + 1];
+      }
+      if (sl == 0) edges += hi - lo;
+      uint32_t len = hi - lo;
+      for (int o = 8; o < 32; o <<= 1) len = max(len, __shfl_xor_sync(0xffffffffu, len, o));
+      if (len <= GROUP_ROW) {
+        for (uint32_t k0 = 0; k0 < len; k0 += 8)
+          bfs_visit(g, lo + k0 + sl, hi, mode, level, kl, ubd, big_row, dist, vis, nxt, ncnt);
+      } else {
+        for (uint32_t x = 0; x < 4; x++) {
+          const uint32_t lx = __shfl_sync(0xffffffffu, lo, x * 8), hx = __shfl_sync(0xffffffffu, hi, x * 8);
+          for (uint32_t k0 = lx; k0 < hx; k0 += 32)
+            bfs_visit(g, k0 + lane, hx, mode, level, kl, ubd, big_row, dist, vis, nxt, ncnt);
+        }
+      }
     }
     cl.sync();
     uint32_t *tmp = cur;
     cur = nxt;
     nxt = tmp;
   }
-  if (lane == 0 && edges) atomicAdd(bytes, edges * 4ull);
+  if (edges) atomicAdd(bytes, edges * 4ull);
   cl.sync();  // every CTA has read the last counts
 }
 
@@ -286,14 +305,35 @@ __device__ uint32_t cluster_build_local_graph(
       if (c > DMASK) atomicOr(&r0->flag, 1u);
     }
   }
-  for (uint32_t i = gw; i < nl; i += gwstride) {
-    const uint32_t v = __ldcg(lgid + i);
-    const uint32_t lo = g.off[v], hi = g.off[v + 1];
-    if (hi - lo >= big_row) continue;
+  for (uint32_t i0 = gw * 4u; i0 < nl; i0 += gwstride * 4u) {
+    // four rows per warp: 8-lane groups when all four are short, else one
+    // after the other by the whole warp; long rows were counted above
+    const uint32_t grp = lane >> 3, sl = lane & 7, i = i0 + grp;
+    uint32_t lo = 0, hi = 0;
+    bool mine = false;  // this group's row is a short one to count here
+    if (i < nl) {
+      const uint32_t v = __ldcg(lgid + i);
+      lo = g.off[v];
+      hi = g.off[v + 1];
+      mine = hi - lo < big_row;
+      if (!mine) hi = lo;
+    }
+    uint32_t len = hi - lo;
+    for (int o = 8; o < 32; o <<= 1) len = max(len, __shfl_xor_sync(0xffffffffu, len, o));
     uint32_t c = 0;
-    for (uint32_t k = lo + lane; k < hi; k += 32) c += bit_cg(comp, g.adj[k]) ? 1u : 0u;
-    for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
-    if (lane == 0) {
+    if (len <= GROUP_ROW) {
+      for (uint32_t k = lo + sl; k < hi; k += 8) c += bit_cg(comp, g.adj[k]) ? 1u : 0u;
+      for (int o = 4; o; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    } else {
+      for (uint32_t x = 0; x < 4; x++) {
+        const uint32_t lx = __shfl_sync(0xffffffffu, lo, x * 8), hx = __shfl_sync(0xffffffffu, hi, x * 8);
+        uint32_t cx = 0;
+        for (uint32_t k = lx + lane; k < hx; k += 32) cx += bit_cg(comp, g.adj[k]) ? 1u : 0u;
+        for (int o = 16; o; o >>= 1) cx += __shfl_xor_sync(0xffffffffu, cx, o);
+        if (grp == x) c = cx;
+      }
+    }
+    if (sl == 0 && mine) {
       loff[i] = (c + 3u) & ~3u;
       fa[i] = c;
       if (c > DMASK) atomicOr(&r0->flag, 1u);
@@ -341,28 +381,69 @@ __device__ uint32_t cluster_build_local_graph(
     for (uint32_t k = wpos + t; k < padded; k += PREP_THREADS) ladj[w0 + k] = SENT;
     if (t == 0) pbytes += 4ull * (hi - lo) + 4ull * padded + 12ull;
   }
-  for (uint32_t i = gw; i < nl; i += gwstride) {
-    const uint32_t v = __ldcg(lgid + i);
-    const uint32_t lo = g.off[v], hi = g.off[v + 1];
-    if (hi - lo >= big_row) continue;
-    const uint32_t w0 = __ldcg(loff + i);
-    uint32_t wpos = 0;
-    for (uint32_t k = lo; k < hi; k += 32) {
-      uint32_t w = 0;
-      bool in = false;
-      if (k + lane < hi) {
-        w = g.adj[k + lane];
-        in = bit_cg(comp, w);
+  for (uint32_t i0 = gw * 4u; i0 < nl; i0 += gwstride * 4u) {
+    // four rows per warp as in the count above; long rows were filled above
+    const uint32_t grp = lane >> 3, sl = lane & 7, i = i0 + grp;
+    uint32_t lo = 0, hi = 0, w0 = 0, padded = 0;
+    bool mine = false;
+    if (i < nl) {
+      const uint32_t v = __ldcg(lgid + i);
+      lo = g.off[v];
+      hi = g.off[v + 1];
+      mine = hi - lo < big_row;
+      if (!mine) {
+        hi = lo;
+      } else {
+        w0 = __ldcg(loff + i);
+        padded = __ldcg(loff + i + 1) - w0;
       }
-      const unsigned m = __ballot_sync(0xffffffffu, in);
-      if (in) ladj[w0 + wpos + __popc(m & lane_lt())] = local_id_cg(comp, wpre, w);
-      wpos += __popc(m);
     }
-    const uint32_t padded = __ldcg(loff + i + 1) - w0;
-    for (uint32_t k = wpos + lane; k < padded; k += 32) ladj[w0 + k] = SENT;
-    if (lane == 0) pbytes += 4ull * (hi - lo) + 4ull * padded + 12ull;
+    uint32_t len = hi - lo;
+    for (int o = 8; o < 32; o <<= 1) len = max(len, __shfl_xor_sync(0xffffffffu, len, o));
+    if (len <= GROUP_ROW) {
+      uint32_t wpos = 0;
+      for (uint32_t k0 = 0; k0 < len; k0 += 8) {
+        const uint32_t k = lo + k0 + sl;
+        uint32_t w = 0;
+        bool in = false;
+        if (k < hi) {
+          w = g.adj[k];
+          in = bit_cg(comp, w);
+        }
+        const uint32_t gm = (__ballot_sync(0xffffffffu, in) >> (grp * 8u)) & 0xFFu;
+        if (in) ladj[w0 + wpos + __popc(gm & ((1u << sl) - 1u))] = local_id_cg(comp, wpre, w);
+        wpos += __popc(gm);
+      }
+      if (mine) {
+        for (uint32_t k = wpos + sl; k < padded; k += 8) ladj[w0 + k] = SENT;
+        if (sl == 0) pbytes += 4ull * (hi - lo) + 4ull * padded + 12ull;
+      }
+    } else {
+      for (uint32_t x = 0; x < 4; x++) {
+        const uint32_t src = x * 8u;
+        if (!__shfl_sync(0xffffffffu, (uint32_t)mine, src)) continue;
+        const uint32_t lx = __shfl_sync(0xffffffffu, lo, src);
+        const uint32_t hx = __shfl_sync(0xffffffffu, hi, src);
+        const uint32_t wx = __shfl_sync(0xffffffffu, w0, src);
+        const uint32_t px = __shfl_sync(0xffffffffu, padded, src);
+        uint32_t wpos = 0;
+        for (uint32_t k = lx; k < hx; k += 32) {
+          uint32_t w = 0;
+          bool in = false;
+          if (k + lane < hx) {
+            w = g.adj[k + lane];
+            in = bit_cg(comp, w);
+          }
+          const unsigned m = __ballot_sync(0xffffffffu, in);
+          if (in) ladj[wx + wpos + __popc(m & lane_lt())] = local_id_cg(comp, wpre, w);
+          wpos += __popc(m);
+        }
+        for (uint32_t k = wpos + lane; k < px; k += 32) ladj[wx + k] = SENT;
+        if (lane == 0) pbytes += 4ull * (hx - lx) + 4ull * px + 12ull;
+      }
+    }
   }
-  if (lane == 0 && pbytes) atomicAdd(bytes, pbytes);
+  if (pbytes) atomicAdd(bytes, pbytes);
   if (t == 0) sh.q_local = local_id_cg(comp, wpre, q);
   cl.sync();
   return nl;
@@ -516,8 +597,15 @@ prep_kernel(DevGraph g, SlotArrays sa, Slot *slots, const PrepJob *jobs,
 cudaError_t launch_prep(uint32_t cluster, cudaStream_t stream, DevGraph g,
                         SlotArrays sa, Slot *slots, const PrepJob *jobs,
                         int njobs, PrepScratch ps, Pool pool, Counters *ctr) {
-  if (cluster != 1 && cluster != 2 && cluster != 4 && cluster != 8) return cudaErrorInvalidValue;
+  if (cluster != 1 && cluster != 2 && cluster != 4 && cluster != 8 && cluster != 16)
+    return cudaErrorInvalidValue;
   if (njobs <= 0) return cudaSuccess;
+  if (cluster > 8) {
+    // 16 CTAs is above the portable cluster size: allowed per kernel
+    const cudaError_t e =
+        cudaFuncSetAttribute(prep_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    if (e != cudaSuccess) return e;
+  }
   cudaLaunchConfig_t cfg{};
   cfg.gridDim = dim3((unsigned)njobs * cluster);
   cfg.blockDim = dim3(PREP_THREADS);

@@ -250,8 +250,9 @@ constexpr int PREP_THREADS = 512;
 constexpr int SEARCH_THREADS = SCS_SEARCH_THREADS;
 constexpr int SEARCH_MINB = SCS_SEARCH_MINB;
 
-// Per-query preparation: one thread-block cluster of `cluster` CTAs (1, 2, 4
-// or 8) per job; prep.cu.
+// Per-query preparation: one thread-block cluster of `cluster` CTAs (1, 2, 4,
+// 8 or 16) per job; prep.cu.  PREP_MAX_CLUSTER is the portable size the
+// engine picks on large graphs.
 constexpr uint32_t PREP_MAX_CLUSTER = 8;
 cudaError_t launch_prep(uint32_t cluster, cudaStream_t stream, DevGraph g,
                         SlotArrays sa, Slot *slots, const PrepJob *jobs,

@@ -72,11 +72,14 @@ def test_prepare_parity(eng_c1, og_c1, oracle_lib):
         assert np.array_equal(dist, ctx.dist)
 
 
-@pytest.mark.parametrize("ctas,big_row", [(2, 4096), (8, 4096), (8, 16), (4, 64), (1, 16)])
+@pytest.mark.parametrize("ctas,big_row", [(2, 4096), (8, 4096), (8, 16), (4, 64), (1, 16),
+                                           (16, 32)])
 def test_cluster_prepare_parity(chunglu_small, og_c1, oracle_lib, ctas, big_row):
     """Preparation by a cluster of CTAs per query gives the oracle's local
     graph bit for bit, with rows of at least big_row entries walked by whole
-    CTAs (16 and 64 make most rows of this graph such rows)."""
+    CTAs (16 to 64 make most rows of this graph such rows); shorter rows go
+    four to a warp in 8-lane groups, or one at a time by the whole warp when
+    one of the four is longer than 64 entries."""
     cases = _prep_cases(og_c1, oracle_lib, 24)
     qs = [(l, h, q, 0, ld) for (l, h, q, ld, kl, ubd) in cases]
     eng = _engine(graph=chunglu_small, limit_queries=len(cases), prep_ctas=ctas,
