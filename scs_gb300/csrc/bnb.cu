@@ -1581,17 +1581,25 @@ __device__ void mark_children(Task &T, Sh &sh) {
   __syncthreads();
 }
 
-// number of skipped list entries before index i for a child
-__device__ __forceinline__ uint32_t skipped_before(const Sh &sh, uint32_t i,
-                                                   uint32_t code) {
+// Which of u* and the d_j lie before list index i: bit j of the result is
+// doms_idx[j] < i, bit 31 us_idx < i.  Computed once per entry for all of
+// its children.
+__device__ __forceinline__ uint32_t marks_before(const Sh &sh, uint32_t i) {
   const uint32_t k = sh.ndoms;
-  uint32_t c = 0;
-  if (code == k + 1 && sh.us_idx < i) c++;
-  for (uint32_t j = 0; j < k; j++) {
-    bool sk = (code == 0 || code == k + 1) ? true : (j + 1 < code);
-    if (sk && sh.doms_idx[j] < i) c++;
-  }
-  return c;
+  uint32_t b = sh.us_idx < i ? 0x80000000u : 0u;
+  for (uint32_t j = 0; j < k; j++) b |= (sh.doms_idx[j] < i ? 1u : 0u) << j;
+  return b;
+}
+
+// Skipped list entries before index i for child `code`, from marks_before's
+// bits: Exclude skips u* and every d_j, Include every d_j, Dom_c the d_j with
+// j < c - 1
+__device__ __forceinline__ uint32_t skipped_from_marks(uint32_t b, uint32_t code,
+                                                       uint32_t k) {
+  const uint32_t doms = b & 0x7FFFFFFFu;
+  if (code == k + 1) return (b >> 31) + __popc(doms);
+  if (code == 0) return __popc(doms);
+  return __popc(doms & ((1u << (code - 1)) - 1u));
 }
 
 __device__ __forceinline__ void child_shape(const Sh &sh, uint32_t code,
@@ -1626,7 +1634,7 @@ __device__ void write_child(Task &T, Sh &sh, uint32_t code, uint32_t *ent_dst,
     uint32_t x = T.list[i];
     uint32_t a = T.aux[x];
     if (child_skip(a, code, k)) continue;
-    uint32_t o = i - skipped_before(sh, i, code);
+    uint32_t o = i - skipped_from_marks(marks_before(sh, i), code, k);
     uint32_t ent, deg;
     child_entry(x, T.W[x], a, code, k, ent, deg);
     ent_dst[o] = ent;
@@ -1664,12 +1672,13 @@ __device__ void write_children(Task &T, Sh &sh, uint32_t code_lo,
     for (int j = 0; j < SCS_LIST_UNROLL; j++) {
       const uint32_t i = i0 + BT * j + t;
       if (xs[j] == SENT) continue;
+      const uint32_t mb = marks_before(sh, i);
       for (uint32_t code = code_lo; code <= code_hi; code++) {
         uint32_t *d = dst[code];
         if (!d || child_skip(as[j], code, k)) continue;
         uint32_t s2, c2;
         child_shape(sh, code, s2, c2);
-        uint32_t o = i - skipped_before(sh, i, code);
+        uint32_t o = i - skipped_from_marks(mb, code, k);
         uint32_t ent, deg;
         child_entry(xs[j], ws[j], as[j], code, k, ent, deg);
         d[REC_HDR + o] = ent;
