@@ -212,6 +212,11 @@ static void heu_worker(scs_engine *E, unsigned tid) {
 
 static int engine_init(scs_engine *E) {
   const scs_config &c = E->cfg;
+  if (c.prep_ctas != 0 && c.prep_ctas != 1 && c.prep_ctas != 2 && c.prep_ctas != 4 &&
+      c.prep_ctas != 8 && c.prep_ctas != 16) {
+    E->err = "prep_ctas must be 0, 1, 2, 4, 8 or 16";
+    return SCS_EINVAL;
+  }
   E->dev = c.device;
   CK(cudaSetDevice(E->dev));
   CK(cudaDeviceGetAttribute(&E->num_sms, cudaDevAttrMultiProcessorCount, E->dev));
@@ -280,11 +285,6 @@ static int engine_init(scs_engine *E) {
   // a cluster per query on large graphs, where one SM's BFS and compaction
   // over the CSR would take a large share of the query's time
   E->prep_cluster = c.prep_ctas ? c.prep_ctas : (n >= (1u << 18) ? PREP_MAX_CLUSTER : 1u);
-  if (E->prep_cluster != 1 && E->prep_cluster != 2 && E->prep_cluster != 4 &&
-      E->prep_cluster != 8 && E->prep_cluster != 16) {
-    E->err = "prep_ctas must be 1, 2, 4, 8 or 16";
-    return SCS_EINVAL;
-  }
   RC(E->dalloc(&ps.dist, (size_t)E->prep_cap * n, false));
   RC(E->dalloc(&ps.vis, (size_t)E->prep_cap * ps.stride_w, false));
   RC(E->dalloc(&ps.comp, (size_t)E->prep_cap * ps.stride_w, false));

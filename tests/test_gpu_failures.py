@@ -127,3 +127,18 @@ def test_local_graph_limit_reports_too_large(chunglu_small):
             assert r["degree"] == r["kl_heuristic"] <= q["degree"]
         else:
             assert r["status"] in (DONE, HEURISTIC) and r["degree"] == q["degree"]
+
+
+def test_invalid_prep_cluster_is_refused(chunglu_small):
+    """A preparation cluster size other than 1, 2, 4, 8 or 16 is refused at
+    creation with an error, and a valid one on the same graph works."""
+    from scs_gb300.engine import Engine, SCSError
+    with pytest.raises(SCSError):
+        Engine(graph=chunglu_small, limit_queries=4, stack_words=1 << 20, pool_words=1 << 24,
+               prep_ctas=3)
+    eng = Engine(graph=chunglu_small, limit_queries=4, stack_words=1 << 20, pool_words=1 << 24,
+                 prep_ctas=2)
+    try:
+        assert eng.solve([(3, 6, 10, 1, 1)])[0]["status"] in (0, 1)
+    finally:
+        eng.close()
