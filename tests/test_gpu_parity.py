@@ -127,6 +127,47 @@ def test_cluster_prepare_rmat_hubs(rmat15, oracle_lib):
         eng.close()
 
 
+@pytest.mark.parametrize("ctas", [8, 16])
+def test_cluster_prepare_large_local_graphs(oracle_lib, ctas):
+    """Local graphs of nearly 200,000 vertices (a 200,000-vertex Chung-Lu
+    graph, exponent 2.3, queries with small incumbents): BFS frontiers of tens
+    of thousands spread over the cluster, and rows of up to a few thousand
+    entries; the local graph equals the oracle's bit for bit."""
+    from scs_gb300 import workloads as W
+    from scs_gb300.engine import Engine
+    n, u, v = W.chung_lu(200000, 4000000, 2.3, seed=11)
+    off, adj = W.to_csr(n, u, v)
+    og = oracle_lib.OracleGraph(n, off, adj)
+    rng = np.random.default_rng(5)
+    cases = []
+    for q in rng.choice(np.flatnonzero(og.core >= 8), size=40, replace=False):
+        q = int(q)
+        h = int(rng.integers(10, 60))
+        l = int(rng.integers(3, h // 2))
+        kl, _ = og.heuristic(0, l, h, q)
+        if kl >= min(int(og.core[q]), h - 1):
+            continue
+        cases.append((l, h, q, 10, kl, int(oracle_lib.lib().orc_ubd_host(kl, h))))
+    cases = cases[:6]
+    assert len(cases) >= 3
+    qs = [(l, h, q, 0, ld) for (l, h, q, ld, kl, ubd) in cases]
+    eng = Engine(csr=(n, off, adj), limit_queries=len(cases), stack_words=1 << 20,
+                 pool_words=1 << 24, prep_ctas=ctas)
+    try:
+        nl, ql = eng.debug_prepare(qs, [c[4] for c in cases], [c[5] for c in cases])
+        assert int(nl.max()) > 10000
+        for i, (l, h, q, ld, kl, ubd) in enumerate(cases):
+            ctx = oracle_lib.OracleCtx(og, l, h, q, kl, ubd, ld)
+            assert int(nl[i]) == ctx.n and int(ql[i]) == ctx.q_local
+            gid, loff, ladj, dist = eng.debug_local_graph(i, int(nl[i]), int(ctx.off[-1]) + 8)
+            assert np.array_equal(gid, ctx.gid)
+            assert np.array_equal(loff, ctx.off)
+            assert np.array_equal(ladj, ctx.adj)
+            assert np.array_equal(dist, ctx.dist)
+    finally:
+        eng.close()
+
+
 def test_cluster_prepare_keeps_answers(chunglu_small, og_c1):
     """Whole searches on local graphs prepared by 8-CTA clusters (rows of 32
     or more entries by whole CTAs) give the golden exact answers."""
