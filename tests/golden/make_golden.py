@@ -14,7 +14,8 @@ the generators is detected instead of silently comparing different graphs.
 Usage: python tests/golden/make_golden.py [heuristic|answers|brute|all]
        python tests/golden/make_golden.py answers_rmat <count> <node_limit>
            (answers_rmat_s15_ef16.json: the mid-size workload's first
-           <count> queries; committed with 96 and 30000)
+           <count> queries; committed with 120 and 200000, about
+           2.5 hours on 8 cores)
 """
 import hashlib
 import json
