@@ -346,7 +346,10 @@ def test_search_rmat_golden(rmat15):
     # them need more than 140,000)
     assert len(gold) >= 14
     rows = [(g["l"], g["h"], g["q"], g["heur"], g["limit_doms"]) for g in gold]
-    eng = _engine(graph=rmat15, limit_queries=len(rows))
+    # the task store sized from device memory, as the bench's engine does: the
+    # hardest of these queries searches more than a hundred thousand tasks on
+    # every CTA at once, beyond the small stores of the other tests
+    eng = _engine(graph=rmat15, limit_queries=len(rows), stack_words=0, pool_words=0)
     try:
         res = eng.solve(rows)
     finally:
