@@ -42,6 +42,10 @@ constexpr int BT = SEARCH_THREADS;
 #ifndef SCS_LIST_UNROLL
 #define SCS_LIST_UNROLL 4
 #endif
+// the same when writing a step's children (one pass writes all of them)
+#ifndef SCS_CHILD_UNROLL
+#define SCS_CHILD_UNROLL 8
+#endif
 // rule-1/2 removals: rows cut into chunks of this many words, 32 rows per
 // warp batch (0: short rows per thread, long rows per warp).  16 measured
 // 1.2 % above 32 on the bench once most row reads hit L2.
@@ -1655,21 +1659,21 @@ __device__ void write_children(Task &T, Sh &sh, uint32_t code_lo,
                                uint32_t code_hi, uint32_t *const *dst) {
   const int t = threadIdx.x;
   const uint32_t s = sh.s, k = sh.ndoms;
-  for (uint32_t i0 = 0; i0 < s; i0 += BT * SCS_LIST_UNROLL) {
-    uint32_t xs[SCS_LIST_UNROLL], as[SCS_LIST_UNROLL], ws[SCS_LIST_UNROLL];
+  for (uint32_t i0 = 0; i0 < s; i0 += BT * SCS_CHILD_UNROLL) {
+    uint32_t xs[SCS_CHILD_UNROLL], as[SCS_CHILD_UNROLL], ws[SCS_CHILD_UNROLL];
 #pragma unroll
-    for (int j = 0; j < SCS_LIST_UNROLL; j++) {
+    for (int j = 0; j < SCS_CHILD_UNROLL; j++) {
       const uint32_t i = i0 + BT * j + t;
       xs[j] = i < s ? T.list[i] : SENT;
     }
 #pragma unroll
-    for (int j = 0; j < SCS_LIST_UNROLL; j++) {
+    for (int j = 0; j < SCS_CHILD_UNROLL; j++) {
       const uint32_t xx = xs[j] != SENT ? xs[j] : 0u;
       as[j] = T.aux[xx];
       ws[j] = T.W[xx];
     }
 #pragma unroll
-    for (int j = 0; j < SCS_LIST_UNROLL; j++) {
+    for (int j = 0; j < SCS_CHILD_UNROLL; j++) {
       const uint32_t i = i0 + BT * j + t;
       if (xs[j] == SENT) continue;
       const uint32_t mb = marks_before(sh, i);
