@@ -563,35 +563,53 @@ bool verify_community(const HostGraph &g, const uint32_t *H, uint32_t hs,
   std::vector<uint32_t> mem(H, H + hs);
   std::sort(mem.begin(), mem.end());
   mem.erase(std::unique(mem.begin(), mem.end()), mem.end());
-  auto in = [&](uint32_t v) { return std::binary_search(mem.begin(), mem.end(), v); };
+  if (mem.back() >= g.n) return false;
+  // Membership by stamp (one array per thread, reused across calls): a row
+  // scan costs one lookup per neighbour, not a binary search.  A hub in H
+  // with thousands of neighbours is common, and results are verified
+  // between search slices.
+  thread_local std::vector<uint32_t> stamp, pos;
+  thread_local uint32_t epoch = 0;
+  if (stamp.size() < g.n) {
+    stamp.assign(g.n, 0);
+    pos.assign(g.n, 0);
+    epoch = 0;
+  }
+  if (++epoch == 0) {
+    std::fill(stamp.begin(), stamp.end(), 0u);
+    epoch = 1;
+  }
+  for (uint32_t i = 0; i < (uint32_t)mem.size(); i++) {
+    stamp[mem[i]] = epoch;
+    pos[mem[i]] = i;
+  }
+  const uint32_t *off = g.off.data(), *adj = g.adj.data();
+  auto in = [&](uint32_t v) { return stamp[v] == epoch; };
   uint32_t mind = UINT32_MAX;
   for (uint32_t v : mem) {
     uint32_t d = 0;
-    for (uint32_t k = g.off[v]; k < g.off[v + 1]; k++) d += in(g.adj[k]);
+    for (uint32_t k = off[v]; k < off[v + 1]; k++) d += in(adj[k]);
     mind = std::min(mind, d);
   }
   md = mind;
-  std::vector<uint32_t> seen{mem[0]}, stack{mem[0]};
+  std::vector<uint32_t> stack{mem[0]};
   std::vector<char> vis(mem.size(), 0);
   vis[0] = 1;
   size_t cnt = 1;
   while (!stack.empty()) {
     uint32_t v = stack.back();
     stack.pop_back();
-    for (uint32_t k = g.off[v]; k < g.off[v + 1]; k++) {
-      auto it = std::lower_bound(mem.begin(), mem.end(), g.adj[k]);
-      if (it != mem.end() && *it == g.adj[k]) {
-        size_t i = (size_t)(it - mem.begin());
-        if (!vis[i]) {
-          vis[i] = 1;
-          cnt++;
-          stack.push_back(*it);
-        }
+    for (uint32_t k = off[v]; k < off[v + 1]; k++) {
+      const uint32_t w = adj[k];
+      if (in(w) && !vis[pos[w]]) {
+        vis[pos[w]] = 1;
+        cnt++;
+        stack.push_back(w);
       }
     }
   }
   bool conn = cnt == mem.size();
-  return conn && in(q) && mem.size() >= l && mem.size() <= h;
+  return conn && q < g.n && in(q) && mem.size() >= l && mem.size() <= h;
 }
 
 }  // namespace scs
