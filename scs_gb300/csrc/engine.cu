@@ -67,6 +67,8 @@ struct SlotHost {
 struct Done {
   scs_result r{};
   std::vector<uint32_t> H;
+  uint64_t t_submit = 0;
+  bool check = true;  // verify H (not for rejected queries)
 };
 
 std::string g_create_error;
@@ -132,7 +134,16 @@ struct scs_engine {
   std::condition_variable heu_cv, heu_done_cv;
   std::vector<std::thread> heu_workers;
   bool heu_stop = false;
+  // Finished queries wait in `verify_q` until the verifier thread has checked
+  // their community against the graph, then move to `done` for scs_poll.
+  // The check runs beside the next search slice instead of between slices.
+  std::deque<Done> verify_q;
   std::deque<Done> done;
+  std::mutex res_mu;  // verify_q, done, res_pending, res_stop
+  std::condition_variable res_cv;
+  size_t res_pending = 0;  // in verify_q or being checked
+  bool res_stop = false;
+  std::thread verifier;
   uint64_t next_ticket = 1;
   uint32_t running = 0;
   uint64_t stats[SCS_STAT_COUNT] = {0};
@@ -209,6 +220,8 @@ static void heu_worker(scs_engine *E, unsigned tid) {
     E->heu_done_cv.notify_all();
   }
 }
+
+static void verify_worker(scs_engine *E);
 
 static int engine_init(scs_engine *E) {
   const scs_config &c = E->cfg;
@@ -402,6 +415,7 @@ static int engine_init(scs_engine *E) {
   E->work.resize(E->host_threads);
   // greedy incumbents of submitted queries are computed by these workers
   for (unsigned k = 0; k < E->host_threads; k++) E->heu_workers.emplace_back(heu_worker, E, k);
+  E->verifier = std::thread(verify_worker, E);
   return 0;
 }
 
@@ -425,6 +439,39 @@ static SearchParams make_params(scs_engine *E) {
   return P;
 }
 
+// Hand a finished query to the verifier thread.
+static void post_result(scs_engine *E, Done &&d) {
+  {
+    std::lock_guard<std::mutex> lk(E->res_mu);
+    E->verify_q.push_back(std::move(d));
+    E->res_pending++;
+  }
+  E->res_cv.notify_one();
+}
+
+// Verifier thread: checks each finished query's community (connected,
+// contains q, l <= |H| <= h, minimum degree equal to the answer), sets
+// h_verified and the latency, and makes the result visible to scs_poll.
+static void verify_worker(scs_engine *E) {
+  std::unique_lock<std::mutex> lk(E->res_mu);
+  for (;;) {
+    E->res_cv.wait(lk, [&] { return E->res_stop || !E->verify_q.empty(); });
+    if (E->verify_q.empty()) return;  // stopping, nothing left
+    Done d = std::move(E->verify_q.front());
+    E->verify_q.pop_front();
+    lk.unlock();
+    uint32_t md = 0;
+    const bool ok = d.check && verify_community(E->g, d.H.data(), (uint32_t)d.H.size(),
+                                                d.r.q, d.r.l, d.r.h, md);
+    d.r.h_verified = (ok && md == d.r.degree) ? 1u : 0u;
+    d.r.latency_ns = now_ns() - d.t_submit;
+    lk.lock();
+    E->done.push_back(std::move(d));
+    E->res_pending--;
+    E->res_cv.notify_all();
+  }
+}
+
 static void finish_result(scs_engine *E, uint32_t si, uint32_t degree,
                           int32_t status, uint64_t nodes, uint64_t search_ns,
                           const std::vector<uint32_t> &H) {
@@ -441,12 +488,8 @@ static void finish_result(scs_engine *E, uint32_t si, uint32_t degree,
   d.r.search_ns = search_ns;
   d.H = H;
   d.r.h_size = (uint32_t)H.size();
-  uint32_t md = 0;
-  bool ok = verify_community(E->g, H.data(), (uint32_t)H.size(), sh.p.q.q,
-                             sh.p.q.l, sh.p.q.h, md);
-  d.r.h_verified = (ok && md == degree) ? 1u : 0u;
-  d.r.latency_ns = now_ns() - sh.p.t_submit;
-  E->done.push_back(std::move(d));
+  d.t_submit = sh.p.t_submit;
+  post_result(E, std::move(d));
   sh.busy = false;
   if (sh.parked) {  // a query whose preparation failed is never released
     sh.parked = false;
@@ -468,13 +511,9 @@ static void finish_now(scs_engine *E, const Pending &p, uint32_t degree,
   d.r.kl_heuristic = kl_heu;
   d.H = H;
   d.r.h_size = (uint32_t)H.size();
-  uint32_t md = 0;
-  bool ok = status != SCS_BAD_QUERY &&
-            verify_community(E->g, H.data(), (uint32_t)H.size(), p.q.q, p.q.l,
-                             p.q.h, md);
-  d.r.h_verified = (ok && md == degree) ? 1u : 0u;
-  d.r.latency_ns = now_ns() - p.t_submit;
-  E->done.push_back(std::move(d));
+  d.t_submit = p.t_submit;
+  d.check = status != SCS_BAD_QUERY;
+  post_result(E, std::move(d));
 }
 
 // Admit queued queries into free slots; returns the number of prep jobs.
@@ -913,12 +952,20 @@ int scs_step(scs_engine *E) {
   int a = admit(E);
   if (a < 0) return a;
   if (E->running > 0) RC(slice(E));
-  size_t queued;
+  size_t queued, checking;
   {
     std::lock_guard<std::mutex> lk(E->heu_mu);
     queued = E->queue.size();
   }
-  return (int)(queued + E->running);
+  {
+    std::unique_lock<std::mutex> lk(E->res_mu);
+    // with nothing left to search, wait for the last checks so that a run
+    // to completion ends with every result pollable
+    if (queued + E->running == 0)
+      E->res_cv.wait(lk, [&] { return E->res_pending == 0; });
+    checking = E->res_pending;
+  }
+  return (int)(queued + E->running + checking);
 }
 
 int scs_run(scs_engine *E) {
@@ -934,6 +981,7 @@ int scs_poll(scs_engine *E, scs_result *out, int max, uint32_t *h_buf,
              uint32_t h_stride) {
   if (!E || (!out && max > 0)) return SCS_EINVAL;
   int k = 0;
+  std::lock_guard<std::mutex> lk(E->res_mu);
   while (k < max && !E->done.empty()) {
     Done &d = E->done.front();
     out[k] = d.r;
@@ -971,6 +1019,12 @@ int scs_destroy(scs_engine *E) {
   }
   E->heu_cv.notify_all();
   for (auto &t : E->heu_workers) t.join();
+  {
+    std::lock_guard<std::mutex> lk(E->res_mu);
+    E->res_stop = true;
+  }
+  E->res_cv.notify_all();
+  if (E->verifier.joinable()) E->verifier.join();
   if (E->stream) cudaStreamSynchronize(E->stream);
   for (void *p : E->allocs) cudaFree(p);
   cudaFree(E->d_mlp_w);
