@@ -282,9 +282,12 @@ def run_reference(args):
 def run_serve(args):
     """Serving mode: queries arrive as a Poisson process at each rate for
     --serve-seconds and are submitted at their arrival times while the engine
-    steps (admission between slices, 5 ms slices unless --slice-us says
-    otherwise).  Latency runs from arrival to the result; throughput is the
-    completed queries over the time to the last result.  One GPU, rank 0."""
+    steps (admission between slices; the engine's 80 ms slices unless
+    --slice-us says otherwise: a slice ends early once nothing is left to
+    search, so long slices cost no latency at low load and save slice
+    boundaries under load).  Latency runs from arrival to the result;
+    throughput is the completed queries over the time to the last result.
+    One GPU, rank 0."""
     rank, world, local = env_rank()
     if rank != 0:
         return 0
@@ -297,7 +300,7 @@ def run_serve(args):
         rng = np.random.default_rng(45)
         arrive = np.cumsum(rng.exponential(1.0 / rate, count))
         eng = Engine(csr=(n, off, adj), limit_queries=args.slots or 256,
-                     slice_us=args.slice_us or 5000,
+                     slice_us=args.slice_us,
                      ctas_per_sm=args.ctas_per_sm, node_budget=args.node_budget,
                      stack_words=args.stack_words, pool_words=args.pool_words, device=local,
                      active_queries=args.active_queries, max_local=args.max_local,
@@ -336,7 +339,7 @@ def run_serve(args):
                 "verified_fraction": sum(1 for r in res if r["h_verified"]) / max(len(res), 1),
                 "data": "synthetic",
                 "config": {"workload": WORKLOADS[_WL[0]][1], "arrival_window_s": args.serve_seconds,
-                           "node_budget": args.node_budget, "slice_us": args.slice_us or 5000,
+                           "node_budget": args.node_budget, "slice_us": args.slice_us or 80000,
                            "active_queries": st["active"], "slots": args.slots or 256,
                            "arm": args.arm if args.arm != "auto" else "plain",
                            "held_by_memory": st["held_memory"],
