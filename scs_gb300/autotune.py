@@ -32,7 +32,8 @@ import numpy as np
 CACHE_DIR = os.environ.get("SCS_TUNE_DIR", os.path.join(os.path.expanduser("~"), ".cache", "scs_gb300"))
 # (ctas_per_sm, active_queries, slice_us, stack_words)
 DEFAULT_GRID = [(3, 32, 80000, 0), (2, 32, 80000, 0), (3, 16, 80000, 0), (3, 64, 80000, 0),
-                (3, 32, 40000, 0), (3, 32, 160000, 0), (3, 32, 80000, 1 << 21)]
+                (3, 128, 80000, 0), (3, 32, 40000, 0), (3, 32, 160000, 0),
+                (3, 32, 80000, 1 << 21)]
 
 
 def graph_key(off, adj, rows):
