@@ -304,6 +304,7 @@ static int engine_init(scs_engine *E) {
   RC(E->dalloc(&ps.fa, (size_t)E->prep_cap * n, false));
   RC(E->dalloc(&ps.fb, (size_t)E->prep_cap * n, false));
   RC(E->dalloc(&ps.wpre, (size_t)E->prep_cap * ps.stride_w, false));
+  RC(E->dalloc(&ps.ldeg, (size_t)E->prep_cap * n, false));
   RC(E->dalloc(&E->d_jobs, E->prep_cap));
   // search grid and shared memory
   int max_optin = 0;

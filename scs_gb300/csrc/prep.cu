@@ -21,8 +21,11 @@
 //     memory and are updated through distributed shared memory;
 //   * the two prefix scans (local ids, row offsets) run over one segment per
 //     CTA, offset by the segment totals the other CTAs hold;
-//   * degree counts and the ordered row fill go warp per row, or CTA per row
-//     for rows of big_row or more.
+//   * the component BFS counts each component vertex's local degree as it
+//     walks the row (every kept neighbour of a component vertex is in the
+//     component), so no separate counting pass reads the rows again;
+//   * the ordered row fill goes warp per row, or CTA per row for rows of
+//     big_row or more.
 // Every phase ends in a cluster barrier (barrier.cluster, in hardware: no
 // software wait).  Data another CTA wrote is read through L2 (__ldcg), so no
 // stale L1 line is seen.  A CTA reads the other CTAs' shared memory only
@@ -134,19 +137,25 @@ constexpr uint32_t GROUP_ROW = 64;
 // Each lane tests adjacency entry k of its row (none when k >= hi; the call
 // is warp-wide).  Appends the newly reached vertices to the next frontier
 // (small ones from the front, those of big_row or more neighbours from the
-// back) and records distances in mode 0.
-__device__ __forceinline__ void bfs_visit(const DevGraph &g, uint32_t k,
-                                          uint32_t hi, int mode, uint32_t level,
-                                          uint32_t kl, uint32_t ubd, uint32_t big_row,
-                                          uint16_t *dist,
-                                          uint32_t *vis, uint32_t *nxt, uint32_t *ncnt) {
+// back) and records distances in mode 0.  In mode 1 it returns 1 when the
+// entry is a neighbour inside the local graph: kept, or q itself.  Every
+// kept neighbour of a vertex of q's component is in the component, so
+// summed over a component vertex's row this is its local degree.
+__device__ __forceinline__ uint32_t bfs_visit(const DevGraph &g, uint32_t k,
+                                              uint32_t hi, int mode, uint32_t level,
+                                              uint32_t kl, uint32_t ubd, uint32_t big_row,
+                                              uint32_t q, uint16_t *dist,
+                                              uint32_t *vis, uint32_t *nxt, uint32_t *ncnt) {
   const int lane = threadIdx.x & 31;
-  bool fresh = false, big = false;
+  bool fresh = false, big = false, local = false;
   uint32_t w = 0;
   if (k < hi) {
     w = g.adj[k];
     bool ok = true;
-    if (mode == 1) ok = g.core[w] > kl && __ldcg(dist + w) <= ubd;
+    if (mode == 1) {
+      ok = g.core[w] > kl && __ldcg(dist + w) <= ubd;
+      local = ok || w == q;
+    }
     const uint32_t bit = 1u << (w & 31);
     if (ok && !(__ldcg(vis + (w >> 5)) & bit)) {
       const uint32_t old = atomicOr(&vis[w >> 5], bit);
@@ -170,6 +179,7 @@ __device__ __forceinline__ void bfs_visit(const DevGraph &g, uint32_t k,
       nxt[bs + __popc(ms & lane_lt())] = w;
     if (mode == 0) dist[w] = (uint16_t)(level + 1);
   }
+  return local ? 1u : 0u;
 }
 
 // Level-synchronous BFS from q over the cluster.  mode 0: whole graph, depth
@@ -180,7 +190,7 @@ __device__ __forceinline__ void bfs_visit(const DevGraph &g, uint32_t k,
 __device__ void cluster_bfs(cg::cluster_group &cl, PrepSh &sh, PrepSh *r0,
                             const DevGraph &g, uint32_t q, int mode, uint32_t maxd,
                             uint32_t kl, uint32_t ubd, uint32_t big_row, uint16_t *dist,
-                            uint32_t *vis, uint32_t *fa, uint32_t *fb,
+                            uint32_t *vis, uint32_t *fa, uint32_t *fb, uint32_t *ldeg,
                             unsigned long long *bytes) {
   const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
   const uint32_t R = cl.num_blocks(), r = cl.block_rank();
@@ -206,8 +216,13 @@ __device__ void cluster_bfs(cg::cluster_group &cl, PrepSh &sh, PrepSh *r0,
       const uint32_t v = __ldcg(cur + (g.n - 1u - b));
       const uint32_t lo = g.off[v], hi = g.off[v + 1];
       if (t == 0) edges += hi - lo;
+      uint32_t c = 0;
       for (uint32_t k0 = lo + (uint32_t)wid * 32u; k0 < hi; k0 += PREP_THREADS)
-        bfs_visit(g, k0 + lane, hi, mode, level, kl, ubd, big_row, dist, vis, nxt, ncnt);
+        c += bfs_visit(g, k0 + lane, hi, mode, level, kl, ubd, big_row, q, dist, vis, nxt, ncnt);
+      if (mode == 1) {
+        c = block_sum_all(c, sh.warp);
+        if (t == 0) ldeg[v] = c;
+      }
     }
     // the others: four per warp, by 8-lane groups when all four rows are
     // short, else one after the other by the whole warp
@@ -222,16 +237,24 @@ __device__ void cluster_bfs(cg::cluster_group &cl, PrepSh &sh, PrepSh *r0,
       if (sl == 0) edges += hi - lo;
       uint32_t len = hi - lo;
       for (int o = 8; o < 32; o <<= 1) len = max(len, __shfl_xor_sync(0xffffffffu, len, o));
+      uint32_t c = 0;  // this group's row: its local degree (mode 1)
       if (len <= GROUP_ROW) {
         for (uint32_t k0 = 0; k0 < len; k0 += 8)
-          bfs_visit(g, lo + k0 + sl, hi, mode, level, kl, ubd, big_row, dist, vis, nxt, ncnt);
+          c += bfs_visit(g, lo + k0 + sl, hi, mode, level, kl, ubd, big_row, q, dist, vis,
+                         nxt, ncnt);
+        for (int o = 4; o; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
       } else {
         for (uint32_t x = 0; x < 4; x++) {
           const uint32_t lx = __shfl_sync(0xffffffffu, lo, x * 8), hx = __shfl_sync(0xffffffffu, hi, x * 8);
+          uint32_t cx = 0;
           for (uint32_t k0 = lx; k0 < hx; k0 += 32)
-            bfs_visit(g, k0 + lane, hx, mode, level, kl, ubd, big_row, dist, vis, nxt, ncnt);
+            cx += bfs_visit(g, k0 + lane, hx, mode, level, kl, ubd, big_row, q, dist, vis,
+                            nxt, ncnt);
+          for (int o = 16; o; o >>= 1) cx += __shfl_xor_sync(0xffffffffu, cx, o);
+          if (grp == x) c = cx;
         }
       }
+      if (mode == 1 && sl == 0 && f0 + grp < ns) ldeg[__ldcg(cur + f0 + grp)] = c;
     }
     cl.sync();
     uint32_t *tmp = cur;
@@ -250,7 +273,7 @@ __device__ void cluster_bfs(cg::cluster_group &cl, PrepSh &sh, PrepSh *r0,
 __device__ uint32_t cluster_build_local_graph(
     cg::cluster_group &cl, PrepSh &sh, PrepSh *r0, const DevGraph &g, uint32_t q,
     uint32_t kl, uint32_t ubd, uint16_t *dist, uint32_t *vis, uint32_t *comp, uint32_t *fa,
-    uint32_t *fb, uint32_t *wpre, uint32_t *lgid, uint16_t *ldist, uint32_t *loff,
+    uint32_t *fb, uint32_t *ldeg, uint32_t *wpre, uint32_t *lgid, uint16_t *ldist, uint32_t *loff,
     uint32_t *ladj, unsigned long long cap_adj, uint32_t max_local, uint32_t big_row,
     unsigned long long *bytes) {
   const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
@@ -265,8 +288,9 @@ __device__ uint32_t cluster_build_local_graph(
   }
   cl.sync();
   // 1. bounded BFS over the whole graph; 2. q's component in the kept set
-  cluster_bfs(cl, sh, r0, g, q, 0, ubd, kl, ubd, big_row, dist, vis, fa, fb, bytes);
-  cluster_bfs(cl, sh, r0, g, q, 1, 0, kl, ubd, big_row, dist, comp, fa, fb, bytes);
+  cluster_bfs(cl, sh, r0, g, q, 0, ubd, kl, ubd, big_row, dist, vis, fa, fb, nullptr, bytes);
+  // the component BFS also counts each component vertex's local degree
+  cluster_bfs(cl, sh, r0, g, q, 1, 0, kl, ubd, big_row, dist, comp, fa, fb, ldeg, bytes);
   // 3. local ids: exclusive prefix of per-word popcounts
   for (uint32_t i = gt; i < nw; i += gstride) wpre[i] = __popc(__ldcg(comp + i));
   if (r == 0 && t == 0) {
@@ -276,8 +300,9 @@ __device__ uint32_t cluster_build_local_graph(
   cl.sync();
   const uint32_t nl = cluster_excl_scan(cl, sh, wpre, nw);
   if (nl > max_local) return UINT32_MAX;
-  // 4. gid and distance per local id; rows of big_row or more entries are
-  // listed in fb for whole CTAs
+  // 4. gid, distance and local degree (counted by the component BFS) per
+  // local id: padded into loff[i], unpadded into fa[i].  Rows of big_row or
+  // more entries are listed in fb for whole CTAs to fill.
   for (uint32_t wi = gt; wi < nw; wi += gstride) {
     uint32_t bits = __ldcg(comp + wi), base = __ldcg(wpre + wi);
     while (bits) {
@@ -286,60 +311,16 @@ __device__ uint32_t cluster_build_local_graph(
       const uint32_t v = wi * 32 + b;
       lgid[base] = v;
       ldist[base] = __ldcg(dist + v);
+      const uint32_t c = __ldcg(ldeg + v);
+      loff[base] = (c + 3u) & ~3u;
+      fa[base] = c;
+      if (c > DMASK) atomicOr(&r0->flag, 1u);
       if (g.off[v + 1] - g.off[v] >= big_row) fb[atomicAdd(&r0->nbig, 1u)] = base;
       base++;
     }
   }
   cl.sync();
   const uint32_t nbig = r0->nbig;
-  //    local degree (padded) into loff[i], unpadded into fa[i]
-  for (uint32_t b = r; b < nbig; b += R) {
-    const uint32_t i = __ldcg(fb + b), v = __ldcg(lgid + i);
-    uint32_t c = 0;
-    for (uint32_t k = g.off[v] + t; k < g.off[v + 1]; k += PREP_THREADS)
-      c += bit_cg(comp, g.adj[k]) ? 1u : 0u;
-    c = block_sum_all(c, sh.warp);
-    if (t == 0) {
-      loff[i] = (c + 3u) & ~3u;
-      fa[i] = c;
-      if (c > DMASK) atomicOr(&r0->flag, 1u);
-    }
-  }
-  for (uint32_t i0 = gw * 4u; i0 < nl; i0 += gwstride * 4u) {
-    // four rows per warp: 8-lane groups when all four are short, else one
-    // after the other by the whole warp; long rows were counted above
-    const uint32_t grp = lane >> 3, sl = lane & 7, i = i0 + grp;
-    uint32_t lo = 0, hi = 0;
-    bool mine = false;  // this group's row is a short one to count here
-    if (i < nl) {
-      const uint32_t v = __ldcg(lgid + i);
-      lo = g.off[v];
-      hi = g.off[v + 1];
-      mine = hi - lo < big_row;
-      if (!mine) hi = lo;
-    }
-    uint32_t len = hi - lo;
-    for (int o = 8; o < 32; o <<= 1) len = max(len, __shfl_xor_sync(0xffffffffu, len, o));
-    uint32_t c = 0;
-    if (len <= GROUP_ROW) {
-      for (uint32_t k = lo + sl; k < hi; k += 8) c += bit_cg(comp, g.adj[k]) ? 1u : 0u;
-      for (int o = 4; o; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
-    } else {
-      for (uint32_t x = 0; x < 4; x++) {
-        const uint32_t lx = __shfl_sync(0xffffffffu, lo, x * 8), hx = __shfl_sync(0xffffffffu, hi, x * 8);
-        uint32_t cx = 0;
-        for (uint32_t k = lx + lane; k < hx; k += 32) cx += bit_cg(comp, g.adj[k]) ? 1u : 0u;
-        for (int o = 16; o; o >>= 1) cx += __shfl_xor_sync(0xffffffffu, cx, o);
-        if (grp == x) c = cx;
-      }
-    }
-    if (sl == 0 && mine) {
-      loff[i] = (c + 3u) & ~3u;
-      fa[i] = c;
-      if (c > DMASK) atomicOr(&r0->flag, 1u);
-    }
-  }
-  cl.sync();
   // the search's state words hold in-task degrees in DMASK
   const uint32_t bad = r0->flag;
   cl.sync();
@@ -467,6 +448,7 @@ prep_kernel(DevGraph g, SlotArrays sa, Slot *slots, const PrepJob *jobs,
   uint32_t *fa = ps.fa + (size_t)jb * ps.stride_n;
   uint32_t *fb = ps.fb + (size_t)jb * ps.stride_n;
   uint32_t *wpre = ps.wpre + (size_t)jb * ps.stride_w;
+  uint32_t *ldeg = ps.ldeg + (size_t)jb * ps.stride_n;
   Slot *sl = slots + job.slot;
   uint32_t *loff = sa.loc_off + (size_t)job.slot * (sa.stride_n + 1);
   uint32_t *ladj = sa.loc_adj + (size_t)job.slot * sa.cap_adj;
@@ -474,7 +456,7 @@ prep_kernel(DevGraph g, SlotArrays sa, Slot *slots, const PrepJob *jobs,
   uint32_t *lgid = sa.loc_gid + (size_t)job.slot * sa.stride_n;
 
   const uint32_t nl = cluster_build_local_graph(
-      cl, sh, r0, g, job.q, job.kl, job.ubd, dist, vis, comp, fa, fb, wpre, lgid, ldist,
+      cl, sh, r0, g, job.q, job.kl, job.ubd, dist, vis, comp, fa, fb, ldeg, wpre, lgid, ldist,
       loff, ladj, sa.cap_adj, min(sa.max_local, sa.stride_n), max(ps.big_row, 1u),
       &ctr->prep_bytes);
   if (nl == UINT32_MAX) {

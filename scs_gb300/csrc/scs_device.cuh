@@ -183,6 +183,7 @@ struct PrepScratch {
   uint32_t *fa;    // [jobs][n]
   uint32_t *fb;    // [jobs][n]
   uint32_t *wpre;  // [jobs][nw+1]
+  uint32_t *ldeg;  // [jobs][n] local degree by global id (prep.cu)
   uint32_t stride_n;
   uint32_t stride_w;
   uint32_t big_row;  // rows this long are walked by a whole CTA (prep.cu)
