@@ -154,12 +154,15 @@ int scs_submit(scs_engine *e, const scs_query *q, uint64_t *ticket);
 
 /* Advance the engine: admit waiting queries into free slots (prepared on the
  * device together), release prepared queries to the search up to
- * active_queries, run one search slice, collect finished queries.  Returns
- * the number of queries still outstanding (queued + admitted), or a negative
- * error. */
+ * active_queries, run one search slice, collect finished queries.  A
+ * collected query's community is verified on a background thread, beside
+ * the next slice, before its result reaches scs_poll.  Returns the number of
+ * queries still outstanding (queued + admitted + being verified), or a
+ * negative error.  With nothing left to search it waits for the last checks,
+ * so a return of 0 means every result is pollable. */
 int scs_step(scs_engine *e);
 
-/* Run until every submitted query has a result. */
+/* Run until every submitted query has a pollable result. */
 int scs_run(scs_engine *e);
 
 /* Drain up to max finished results.  For result i the community's global
