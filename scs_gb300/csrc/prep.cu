@@ -17,7 +17,9 @@
 // CTA; here the CTAs of one cluster share the work of a query, so a graph
 // with millions of vertices is not walked by one SM:
 //   * BFS levels: frontier vertices go to warps, those of big_row or more
-//     neighbours (PrepScratch::big_row) to whole CTAs; the frontier counters live in rank 0's shared
+//     neighbours (PrepScratch::big_row) to whole CTAs; a level whose
+//     frontier holds more than n/64 vertices runs bottom-up instead (every
+//     unvisited vertex looks for a neighbour in the frontier); the frontier counters live in rank 0's shared
 //     memory and are updated through distributed shared memory;
 //   * the two prefix scans (local ids, row offsets) run over one segment per
 //     CTA, offset by the segment totals the other CTAs hold;
@@ -211,6 +213,54 @@ __device__ void cluster_bfs(cg::cluster_group &cl, PrepSh &sh, PrepSh *r0,
     if (ns + nb == 0 || (mode == 0 && level >= maxd)) break;
     if (r == 0 && t == 0) sh.cnt[(level + 2) % 3][0] = sh.cnt[(level + 2) % 3][1] = 0;
     uint32_t *ncnt = r0->cnt[(level + 1) % 3];
+    if (mode == 0 && ns + nb > (g.n >> 6) + 32u) {
+      // Large frontier: bottom-up.  Every unvisited vertex scans its row
+      // for a neighbour at distance `level` and stops at the first one
+      // (Beamer's direction-optimizing BFS).  Distances are the same as
+      // top-down; far fewer edges are read when most of the graph is near.
+      for (uint32_t b0 = r * PREP_THREADS + (uint32_t)wid * 32u; b0 < g.n;
+           b0 += R * PREP_THREADS) {
+        const uint32_t v = b0 + lane;
+        bool fresh = false, big = false;
+        if (v < g.n && !((__ldcg(vis + (v >> 5)) >> (v & 31)) & 1u)) {
+          const uint32_t lo = g.off[v], hi = g.off[v + 1];
+          uint32_t k = lo;
+          for (; k < hi; k++)
+            if (__ldcg(dist + g.adj[k]) == level) {
+              fresh = true;
+              break;
+            }
+          edges += (k < hi ? k + 1 : hi) - lo;
+          if (fresh) {
+            dist[v] = (uint16_t)(level + 1);
+            big = hi - lo >= big_row;
+          }
+        }
+        // the warp's 32 vertices share one visited word (b0 is a multiple of 32)
+        const unsigned fm = __ballot_sync(0xffffffffu, fresh);
+        if (lane == 0 && fm) atomicOr(&vis[b0 >> 5], fm);
+        const unsigned ms = __ballot_sync(0xffffffffu, fresh && !big);
+        const unsigned mb = __ballot_sync(0xffffffffu, big);
+        uint32_t bs = 0, bb = 0;
+        if (lane == 0) {
+          if (ms) bs = atomicAdd(&ncnt[0], (uint32_t)__popc(ms));
+          if (mb) bb = atomicAdd(&ncnt[1], (uint32_t)__popc(mb));
+        }
+        bs = __shfl_sync(0xffffffffu, bs, 0);
+        bb = __shfl_sync(0xffffffffu, bb, 0);
+        if (fresh) {
+          if (big)
+            nxt[g.n - 1u - (bb + __popc(mb & lane_lt()))] = v;
+          else
+            nxt[bs + __popc(ms & lane_lt())] = v;
+        }
+      }
+      cl.sync();
+      uint32_t *tmp = cur;
+      cur = nxt;
+      nxt = tmp;
+      continue;
+    }
     // frontier vertices with long rows: a CTA each
     for (uint32_t b = r; b < nb; b += R) {
       const uint32_t v = __ldcg(cur + (g.n - 1u - b));
